@@ -1,0 +1,212 @@
+/*
+ * pd_gb300.h — C ABI of the GB300-native Projective Dynamics substep.
+ *
+ * Two drop-in surfaces, both plain C (pointers, sizes, status codes; no C++ or torch types):
+ *
+ *  1. pd_solver_*  replaces the reference's global-step solver interface
+ *     IGlobalSolver / EigenDirectSolver (core/solver/IGlobalSolver.h:45-127,
+ *     core/solver/EigenDirectSolver.h:33-54): analyze / factorize / analyzed / solve /
+ *     parallelComponents / solveComponent / noteSolveStage / stats. The LDLᵀ factor is computed
+ *     on the host once per factorize; every solve runs on the GPU.
+ *
+ *  2. pd_sim_*  replaces the reference's whole substep, stepOnce(SimContext&)
+ *     (core/sim/Integrator.h:14-38, core/sim/Integrator.cpp:312-797), configured by the
+ *     SceneConfig knobs (core/sim/Scene.h:14-137). The entire substep — predict, K PD iterations
+ *     (projection, scatter with pin elimination, pinned-row overwrite, triangular solves,
+ *     residual gate), velocity update — runs on the GPU; a batch of cloths runs in one launch.
+ *
+ * Errors: every function returns PD_OK (0) or a PD_ERR_* code; pd_last_error() returns the
+ * message of the calling thread's last failure. Where the reference prints and abort()s on a
+ * violated precondition (EigenDirectSolver.cpp:304-314, 363-400), these functions return
+ * PD_ERR_INVALID_ARGUMENT / PD_ERR_STATE instead. A factorization failure
+ * (EigenDirectSolver.cpp:284-291) returns PD_ERR_FACTORIZATION and leaves the object unready.
+ *
+ * Threading: a handle is used by one host thread at a time. All device work of a handle is
+ * ordered on the handle's CUDA stream.
+ */
+#ifndef PD_GB300_H
+#define PD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PD_OK 0
+#define PD_ERR_INVALID_ARGUMENT 1
+#define PD_ERR_STATE 2
+#define PD_ERR_FACTORIZATION 3
+#define PD_ERR_CUDA 4
+#define PD_ERR_UNSUPPORTED 5
+#define PD_ERR_NO_MEMORY 6
+
+/* Arithmetic of the GPU substep. */
+#define PD_PRECISION_FP64_EXACT 0 /* FP64, reference operation order, bit-identical to the CPU path */
+
+/* Mirror of SceneConfig (core/sim/Scene.h:14-137) plus the fields the synthetic scenes need. */
+typedef struct pd_scene_config {
+  double dt;                 /* substep h (default 1/120) */
+  int32_t substeps_per_frame;
+  double gravity[3];         /* default (0, -9.81, 0) */
+  double stiffness;          /* distance constraint κ (default 2300) */
+  double density;            /* edge-lumped mass density (default 1) */
+  double velocity_damping;   /* k_d (default 0.02) */
+  int32_t max_iterations;    /* PD iterations per substep (default 10) */
+  double rel_tolerance;      /* displacement gate, used when residual_tolerance <= 0 */
+  double abs_tolerance;
+  double residual_tolerance; /* residual gate, × |g| (default 1e-3); <= 0 disables */
+  int32_t grid_nx, grid_ny;  /* regular grid (default 40 × 40) */
+  double grid_spacing;       /* default 0.025 */
+  double shear_stiffness;    /* > 0: one diagonal per quad (Mesh::addShearDiagonals) */
+  double bend_stiffness;     /* > 0: midpoint bend stencils (Mesh::addBendingStencils) */
+  int32_t bend_sampling;     /* 0 standard, 1 rows, 2 cols, 3 checkerboard */
+  int32_t bend_stride;       /* >= 1 */
+  int32_t mass_mode;         /* 0: reference edge-lumped masses; 1: uniform, total_mass split evenly */
+  double total_mass;
+  int32_t pin_mode;          /* 0: corners of row ny-1 (reference default); 1: corners of row 0;
+                                2: whole row ny-1; 3: corner (0, ny-1); 4: none */
+  int32_t precision;         /* PD_PRECISION_* */
+} pd_scene_config;
+
+/* Borrowed host arrays describing one cloth; vectors are [x,y,z] interleaved per vertex.
+ * velocities / pin_positions may be NULL (zero velocity; pins at the current positions, as
+ * refreshPinPositions does, core/sim/Scene.cpp:202-207). */
+typedef struct pd_mesh {
+  int32_t n_vertices;
+  const double* positions;
+  const double* velocities;
+  const double* masses;
+  const uint8_t* pinned;
+  const double* pin_positions;
+  int32_t n_edges;
+  const int32_t* edges;        /* 2 per edge (a, b) */
+  const double* edge_rest;
+  const double* edge_stiffness;
+  int32_t n_bends;
+  const int32_t* bends;        /* 3 per stencil (a, b, c), b the middle vertex */
+  const double* bend_stiffness;
+} pd_mesh;
+
+/* Message of this thread's last failure ("" if none). */
+const char* pd_last_error(void);
+/* Fills the SceneConfig defaults (core/sim/Scene.h:14-137). */
+void pd_scene_config_default(pd_scene_config* cfg);
+
+/* ---- Scene construction: Mesh::makeGrid + makeScene (core/mesh/Mesh.cpp:12-54,155-285,
+ *      core/sim/Scene.cpp:39-177). Call pd_grid_counts to size the arrays first. ---- */
+int pd_grid_counts(const pd_scene_config* cfg, int32_t* n_vertices, int32_t* n_edges, int32_t* n_bends);
+int pd_make_grid(const pd_scene_config* cfg, double* positions, double* masses, uint8_t* pinned,
+                 int32_t* edges, double* edge_rest, double* edge_stiffness, int32_t* bends,
+                 double* bend_stiffness);
+
+/* ---- Global solver: IGlobalSolver (core/solver/IGlobalSolver.h:45-127) ---- */
+typedef struct pd_solver pd_solver;
+
+typedef struct pd_solver_stats {   /* IGlobalSolver::Stats (core/solver/IGlobalSolver.h:114-126) */
+  int32_t analyze_calls;
+  int32_t factorize_calls;
+  int32_t solve_calls;
+  double last_analyze_seconds;
+  double last_factorize_seconds;
+  double last_solve_seconds;
+  double total_factorize_seconds;
+  double total_solve_seconds;
+  int64_t nnz;                     /* nonzeros of the analysed 3n × 3n matrix */
+  int64_t factor_nnz;              /* nonzeros of the scalar factor (shared by x, y, z) */
+} pd_solver_stats;
+
+int pd_solver_create(pd_solver** out);
+int pd_solver_destroy(pd_solver* s);
+/* IGlobalSolver::analyze(n, patternMatrix) (:57): symbolic work on the CSC pattern of the
+ * n × n matrix (Eigen's compressed column layout; both triangles or the lower one). */
+int pd_solver_analyze(pd_solver* s, int32_t n, const int32_t* col_ptr, const int32_t* row_idx);
+/* IGlobalSolver::factorize(L) (:60): numeric LDLᵀ on the host, factor uploaded to the GPU.
+ * The structure must equal the analysed one. Requires L = Ã ⊗ I₃ (every 3 × 3 block a scalar
+ * times I₃), which holds for every energy term of this path; otherwise PD_ERR_UNSUPPORTED. */
+int pd_solver_factorize(pd_solver* s, int32_t n, const int32_t* col_ptr, const int32_t* row_idx,
+                        const double* values);
+/* IGlobalSolver::analyzed() (:63): 1 after a successful analyze. */
+int pd_solver_analyzed(const pd_solver* s);
+/* IGlobalSolver::solve(b, x) (:66): host vectors of length n; blocks until x is written. */
+int pd_solver_solve(pd_solver* s, const double* b, double* x);
+/* IGlobalSolver::parallelComponents() (:85): 3 for L = Ã ⊗ I₃. */
+int pd_solver_parallel_components(const pd_solver* s);
+/* IGlobalSolver::solveComponent(c, b, x) (:94-97): writes only entries 3v+c of x. */
+int pd_solver_solve_component(pd_solver* s, int32_t c, const double* b, double* x);
+/* IGlobalSolver::noteSolveStage(seconds) (:111). */
+int pd_solver_note_solve_stage(pd_solver* s, double seconds);
+/* IGlobalSolver::stats() (:126). */
+int pd_solver_stats_get(const pd_solver* s, pd_solver_stats* out);
+
+/* ---- Fused substep: stepOnce (core/sim/Integrator.cpp:312-797) ---- */
+typedef struct pd_sim pd_sim;
+
+typedef struct pd_sim_info {
+  int32_t n_vertices, n_edges, n_bends;
+  int32_t color_count;
+  int64_t matrix_nnz;            /* scalar Ã (n × n) */
+  int64_t factor_nnz;            /* strictly lower scalar factor */
+  int32_t forward_levels, backward_levels;
+  int32_t factorize_count;       /* SimContext::factorizeCount */
+  int32_t analyze_count;
+  int64_t device_bytes;          /* device memory held by this instance */
+} pd_sim_info;
+
+typedef struct pd_sim_stats {    /* SimContext counters (core/sim/Scene.h:161-169) */
+  int32_t iterations_used;       /* of the last substep */
+  int32_t converged;             /* last substep met the gate */
+  int32_t early_exit_count;      /* accumulated */
+  double last_residual;          /* m/s², -1 when the residual gate is disabled */
+} pd_sim_stats;
+
+/* Builds one cloth: validates and copies the arrays, colours the edges, assembles L, orders,
+ * factorizes (one numeric factorization) and uploads everything to the GPU. */
+int pd_sim_create(const pd_mesh* mesh, const pd_scene_config* cfg, pd_sim** out);
+/* Builds a batch of independent cloths (per-instance meshes and configs) run in one launch. */
+int pd_sim_create_batch(int32_t count, const pd_mesh* meshes, const pd_scene_config* cfgs, pd_sim** out);
+int pd_sim_destroy(pd_sim* s);
+int pd_sim_instance_count(const pd_sim* s);
+/* Enqueues `substeps` substeps of every instance on the handle's stream and returns. */
+int pd_sim_step(pd_sim* s, int32_t substeps);
+int pd_sim_synchronize(pd_sim* s);
+/* Uses a caller-owned cudaStream_t (passed as void*) for all later work; NULL = default stream. */
+int pd_sim_set_stream(pd_sim* s, void* cuda_stream);
+/* Copies positions / velocities (3n, nullable) of one instance to / from the host; the get
+ * waits for the handle's queued work. */
+int pd_sim_get_state(pd_sim* s, int32_t instance, double* positions, double* velocities);
+int pd_sim_set_state(pd_sim* s, int32_t instance, const double* positions, const double* velocities);
+/* Device addresses of an instance's position / velocity arrays (3n doubles each). */
+int pd_sim_device_state(pd_sim* s, int32_t instance, double** positions, double** velocities);
+/* Moves pin targets; only the RHS changes, no refactorization (core/assemble/Assembler.h:52-60). */
+int pd_sim_set_pin_positions(pd_sim* s, int32_t instance, const double* pin_positions);
+/* Changes edge stiffnesses; refactorizes (the stamp changes, Assembler.cpp:111-147). */
+int pd_sim_set_edge_stiffness(pd_sim* s, int32_t instance, const double* edge_stiffness);
+/* Changes the pin mask; re-analyzes and refactorizes (Assembler.cpp:149-174). */
+int pd_sim_set_pinned(pd_sim* s, int32_t instance, const uint8_t* pinned, const double* pin_positions);
+/* Replaces the stepping knobs of every instance (dt change ⇒ refactorization). */
+int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg);
+int pd_sim_get_info(pd_sim* s, int32_t instance, pd_sim_info* out);
+int pd_sim_get_stats(pd_sim* s, int32_t instance, pd_sim_stats* out);
+/* Per-substep iteration counts / gate flags of the last pd_sim_step (count = its substeps). */
+int pd_sim_iteration_log(pd_sim* s, int32_t instance, int32_t* iterations, uint8_t* converged, int32_t count);
+/* Exports the factor (perm[n], colptr[n+1], rowidx[nnz], val[nnz], dinv[n]; NULL parts skipped);
+ * *nnz receives the nonzero count. */
+int pd_sim_get_factor(pd_sim* s, int32_t instance, int32_t* perm, int32_t* colptr, int32_t* rowidx,
+                      double* val, double* dinv, int64_t* nnz);
+/* Runs one 3-column solve with the instance's factor: b, x host arrays of 3n. */
+int pd_sim_solve(pd_sim* s, int32_t instance, const double* b, double* x);
+
+/* ---- Host-only inspection (no GPU work): the preparation pd_sim_create performs ---- */
+/* Assembles L, orders and factorizes as pd_sim_create does; exports the factor like
+ * pd_sim_get_factor (call once with NULL arrays to read *nnz) and fills *info (nullable). */
+int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* perm, int32_t* colptr,
+                    int32_t* rowidx, double* val, double* dinv, int64_t* nnz, pd_sim_info* info);
+/* Edge colouring (color_of[n_edges]) of the scene; returns the colour count in *colors. */
+int pd_scene_coloring(const pd_mesh* mesh, uint32_t* color_of, int32_t* colors);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,16 @@
+"""GB300-native Projective Dynamics substep (pd_ipc's per-substep loop) behind a C ABI.
+
+The compute path is the in-tree CUDA library ``pd_gb300/_lib/libpd_gb300.so`` (built by
+``pd_gb300.build``); this package only binds it. There is no CPU fallback: importing the
+bindings raises if the library is missing.
+"""
+from .api import (  # noqa: F401
+    PD_PRECISION_FP64_EXACT,
+    PdError,
+    SceneConfig,
+    GridScene,
+    Simulator,
+    GpuDirectSolver,
+    load_library,
+    make_grid,
+)

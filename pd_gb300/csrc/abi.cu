@@ -1,0 +1,979 @@
+// abi.cu — the C ABI of include/pd_gb300.h: instance build, device arena, sim and solver handles.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <iterator>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/pd_gb300.h"
+#include "device.cuh"
+#include "host.hpp"
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg) {
+  g_lastError = msg;
+  return code;
+}
+int cudaFail(cudaError_t e, const char* what) {
+  return fail(PD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define PD_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cudaFail(e_, #call);  \
+  } while (0)
+
+using Clock = std::chrono::steady_clock;
+double secondsSince(Clock::time_point t0) {
+  return std::chrono::duration<double>(Clock::now() - t0).count();
+}
+
+pdg::GridSpec gridSpecOf(const pd_scene_config& c) {
+  pdg::GridSpec g;
+  g.nx = c.grid_nx;
+  g.ny = c.grid_ny;
+  g.spacing = c.grid_spacing;
+  g.stiffness = c.stiffness;
+  g.density = c.density;
+  g.shearStiffness = c.shear_stiffness;
+  g.bendStiffness = c.bend_stiffness;
+  g.bendSampling = c.bend_sampling;
+  g.bendStride = c.bend_stride;
+  g.massMode = c.mass_mode;
+  g.totalMass = c.total_mass;
+  g.pinMode = c.pin_mode;
+  return g;
+}
+
+// ------------------------------------------------------------------------------ device arena
+// All arrays of all instances of a handle live in one device allocation, uploaded with one copy.
+struct Arena {
+  std::vector<uint8_t> host;
+  size_t add(const void* src, size_t bytes) {
+    const size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + (bytes ? bytes : 1), 0);
+    if (src && bytes) std::memcpy(host.data() + off, src, bytes);
+    return off;
+  }
+  template <class T>
+  size_t add(const std::vector<T>& v) {
+    return add(v.data(), v.size() * sizeof(T));
+  }
+  size_t zeros(size_t bytes) { return add(nullptr, bytes); }
+};
+
+// One cloth: host preparation plus the offsets of its device arrays.
+struct Instance {
+  pdg::Scene scene;
+  pd_scene_config cfg{};
+  pdg::Topology topo;
+  pdg::ScalarMatrix L;
+  pdg::Factor F;
+  pdg::Stamp stamp;
+  std::vector<double> bendRhs;
+  int factorizeCount = 0, analyzeCount = 0;
+  // arena offsets
+  size_t oX, oV, oXn, oXhat, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
+      oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
+      oEarly, oIters, oConv;
+  size_t bytes = 0;
+};
+
+std::string prepare(Instance& I, bool reanalyze) {
+  const auto& c = I.cfg;
+  if (!(c.dt > 0.0)) return "dt must be positive";
+  if (c.max_iterations < 0) return "max_iterations must be >= 0";
+  if (c.precision != PD_PRECISION_FP64_EXACT) return "unsupported precision mode";
+  std::string err = pdg::validateScene(I.scene);
+  if (!err.empty()) return err;
+  pdg::assembleMatrix(I.scene, c.dt, I.L);
+  std::vector<int32_t> perm;
+  if (reanalyze || I.F.perm.empty()) {
+    perm = pdg::nestedDissection(I.scene, I.L);
+    I.analyzeCount += 1;
+  } else {
+    perm = I.F.perm;
+  }
+  if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
+  I.factorizeCount += 1;
+  pdg::assembleBendingRhs(I.scene, I.bendRhs);
+  I.stamp = pdg::computeStamp(I.scene, c.dt);
+  return {};
+}
+
+void layout(Instance& I, Arena& A) {
+  const auto& s = I.scene;
+  const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
+  const size_t before = A.host.size();
+  I.oX = A.add(s.x);
+  I.oV = A.add(s.v);
+  I.oXn = A.zeros(24 * n);
+  I.oXhat = A.zeros(24 * n);
+  I.oBbase = A.zeros(24 * n);
+  I.oM = A.add(s.m);
+  I.oPin = A.add(s.pinned);
+  I.oQ = A.add(s.q);
+  I.oBend = A.add(I.bendRhs);
+  std::vector<int32_t> eab(2 * ne);
+  std::vector<double> rest(ne), k(ne);
+  for (size_t e = 0; e < ne; ++e) {
+    eab[2 * e] = s.edges[e].a;
+    eab[2 * e + 1] = s.edges[e].b;
+    rest[e] = s.edges[e].rest;
+    k[e] = s.edges[e].k;
+  }
+  I.oEab = A.add(eab);
+  I.oRest = A.add(rest);
+  I.oK = A.add(k);
+  I.oKd = A.zeros(24 * ne);
+  I.oRc = A.zeros(24 * ne);
+  I.oSs = A.add(I.topo.sstart);
+  I.oSi = A.add(I.topo.sinc);
+  I.oRs = A.add(I.topo.rstart);
+  I.oRi = A.add(I.topo.rinc);
+  I.oBs = A.add(I.topo.bstart);
+  I.oBi = A.add(I.topo.binc);
+  I.oBf = A.add(I.topo.bfac);
+  std::vector<int32_t> babc(3 * nb);
+  for (size_t b = 0; b < nb; ++b) {
+    babc[3 * b] = s.bends[b].a;
+    babc[3 * b + 1] = s.bends[b].b;
+    babc[3 * b + 2] = s.bends[b].c;
+  }
+  I.oBabc = A.add(babc);
+  I.oIperm = A.add(I.F.iperm);
+  I.oLrp = A.add(I.F.rowptr);
+  I.oLci = A.add(I.F.colidx);
+  I.oLrv = A.add(I.F.rowval);
+  I.oLcp = A.add(I.F.colptr);
+  I.oLri = A.add(I.F.rowidx);
+  I.oLcv = A.add(I.F.colval);
+  I.oDinv = A.add(I.F.dinv);
+  I.oFp = A.add(I.F.fwdLevelPtr);
+  I.oFr = A.add(I.F.fwdRows);
+  I.oBp = A.add(I.F.bwdLevelPtr);
+  I.oBr = A.add(I.F.bwdRows);
+  I.oW = A.zeros(24 * n);
+  const double minusOne = -1.0;
+  I.oLastRes = A.add(&minusOne, sizeof(double));
+  I.oEarly = A.zeros(4);
+  I.oIters = A.zeros(4);
+  I.oConv = A.zeros(4);
+  I.bytes = A.host.size() - before;
+}
+
+pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog) {
+  auto P = [&](size_t off) { return base + off; };
+  const auto& c = I.cfg;
+  const auto& s = I.scene;
+  pdg::InstanceDev d{};
+  d.n = s.n;
+  d.ne = static_cast<int32_t>(s.edges.size());
+  d.nb = static_cast<int32_t>(s.bends.size());
+  d.nlevF = static_cast<int32_t>(I.F.fwdLevelPtr.size()) - 1;
+  d.nlevB = static_cast<int32_t>(I.F.bwdLevelPtr.size()) - 1;
+  d.maxIter = c.max_iterations;
+  d.useResidual = c.residual_tolerance > 0.0 ? 1 : 0;
+  d.hasBendRhs = s.bends.empty() ? 0 : 1;
+  const double h = c.dt;
+  d.h = h;
+  d.invH2 = 1.0 / (h * h);
+  d.dampInvH = (1.0 - c.velocity_damping) * (1.0 / h);
+  for (int k = 0; k < 3; ++k) d.gh2[k] = c.gravity[k] * (h * h);
+  const double gl = std::sqrt(c.gravity[0] * c.gravity[0] + c.gravity[1] * c.gravity[1] + c.gravity[2] * c.gravity[2]);
+  d.gScaleHH = gl * h * h;
+  d.resThreshold = c.residual_tolerance * ((gl < 1.0e-12) ? 1.0e-12 : gl);
+  d.relTol = c.rel_tolerance;
+  d.absTol = c.abs_tolerance;
+  d.x = reinterpret_cast<double*>(P(I.oX));
+  d.v = reinterpret_cast<double*>(P(I.oV));
+  d.xn = reinterpret_cast<double*>(P(I.oXn));
+  d.xhat = reinterpret_cast<double*>(P(I.oXhat));
+  d.bbase = reinterpret_cast<double*>(P(I.oBbase));
+  d.m = reinterpret_cast<const double*>(P(I.oM));
+  d.pinned = reinterpret_cast<const uint8_t*>(P(I.oPin));
+  d.q = reinterpret_cast<const double*>(P(I.oQ));
+  d.bendRhs = reinterpret_cast<const double*>(P(I.oBend));
+  d.eab = reinterpret_cast<const int32_t*>(P(I.oEab));
+  d.erest = reinterpret_cast<const double*>(P(I.oRest));
+  d.ek = reinterpret_cast<const double*>(P(I.oK));
+  d.kd = reinterpret_cast<double*>(P(I.oKd));
+  d.rc = reinterpret_cast<double*>(P(I.oRc));
+  d.sstart = reinterpret_cast<const int32_t*>(P(I.oSs));
+  d.sinc = reinterpret_cast<const int32_t*>(P(I.oSi));
+  d.rstart = reinterpret_cast<const int32_t*>(P(I.oRs));
+  d.rinc = reinterpret_cast<const int32_t*>(P(I.oRi));
+  d.bstart = reinterpret_cast<const int32_t*>(P(I.oBs));
+  d.binc = reinterpret_cast<const int32_t*>(P(I.oBi));
+  d.bfac = reinterpret_cast<const double*>(P(I.oBf));
+  d.babc = reinterpret_cast<const int32_t*>(P(I.oBabc));
+  d.iperm = reinterpret_cast<const int32_t*>(P(I.oIperm));
+  d.Lrp = reinterpret_cast<const int32_t*>(P(I.oLrp));
+  d.Lci = reinterpret_cast<const int32_t*>(P(I.oLci));
+  d.Lrv = reinterpret_cast<const double*>(P(I.oLrv));
+  d.Lcp = reinterpret_cast<const int32_t*>(P(I.oLcp));
+  d.Lri = reinterpret_cast<const int32_t*>(P(I.oLri));
+  d.Lcv = reinterpret_cast<const double*>(P(I.oLcv));
+  d.dinv = reinterpret_cast<const double*>(P(I.oDinv));
+  d.fwdPtr = reinterpret_cast<const int32_t*>(P(I.oFp));
+  d.fwdRows = reinterpret_cast<const int32_t*>(P(I.oFr));
+  d.bwdPtr = reinterpret_cast<const int32_t*>(P(I.oBp));
+  d.bwdRows = reinterpret_cast<const int32_t*>(P(I.oBr));
+  d.w = reinterpret_cast<double*>(P(I.oW));
+  d.iterLog = iterLog;
+  d.convLog = convLog;
+  d.lastResidual = reinterpret_cast<double*>(P(I.oLastRes));
+  d.earlyExits = reinterpret_cast<int32_t*>(P(I.oEarly));
+  d.iterationsUsed = reinterpret_cast<int32_t*>(P(I.oIters));
+  d.converged = reinterpret_cast<int32_t*>(P(I.oConv));
+  return d;
+}
+
+constexpr int kMaxSmem = 200 * 1024;
+
+// Status code of a preparation failure message.
+int prepareCode(const std::string& err) {
+  if (err.find("pivot") != std::string::npos) return PD_ERR_FACTORIZATION;
+  if (err.find("precision") != std::string::npos) return PD_ERR_UNSUPPORTED;
+  return PD_ERR_INVALID_ARGUMENT;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ sim handle
+struct pd_sim {
+  std::vector<Instance> inst;
+  cudaStream_t stream = nullptr;
+  uint8_t* dArena = nullptr;
+  size_t arenaBytes = 0;
+  pdg::InstanceDev* dDesc = nullptr;
+  int32_t* dIterLog = nullptr;
+  uint8_t* dConvLog = nullptr;
+  int logCapacity = 0;
+  int lastSubsteps = 0;
+  int smemBytes = 0;
+
+  ~pd_sim() { release(); }
+  void release() {
+    if (dArena) cudaFree(dArena);
+    if (dDesc) cudaFree(dDesc);
+    if (dIterLog) cudaFree(dIterLog);
+    if (dConvLog) cudaFree(dConvLog);
+    dArena = nullptr;
+    dDesc = nullptr;
+    dIterLog = nullptr;
+    dConvLog = nullptr;
+    logCapacity = 0;
+  }
+
+  int upload(int capacity) {
+    Arena A;
+    for (auto& I : inst) layout(I, A);
+    release();
+    PD_CUDA(cudaMalloc(&dArena, A.host.size()));
+    arenaBytes = A.host.size();
+    PD_CUDA(cudaMemcpy(dArena, A.host.data(), A.host.size(), cudaMemcpyHostToDevice));
+    return ensureLogs(capacity);
+  }
+
+  int ensureLogs(int capacity) {
+    if (capacity <= logCapacity && dDesc) return PD_OK;
+    if (dIterLog) cudaFree(dIterLog);
+    if (dConvLog) cudaFree(dConvLog);
+    dIterLog = nullptr;
+    dConvLog = nullptr;
+    const size_t count = inst.size();
+    PD_CUDA(cudaMalloc(&dIterLog, sizeof(int32_t) * count * capacity));
+    PD_CUDA(cudaMalloc(&dConvLog, count * capacity));
+    PD_CUDA(cudaMemset(dIterLog, 0, sizeof(int32_t) * count * capacity));
+    PD_CUDA(cudaMemset(dConvLog, 0, count * capacity));
+    logCapacity = capacity;
+    return writeDescriptors();
+  }
+
+  int writeDescriptors() {
+    std::vector<pdg::InstanceDev> desc;
+    int smem = 0;
+    for (size_t i = 0; i < inst.size(); ++i) {
+      desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
+      const int need = 24 * inst[i].scene.n;
+      if (need <= kMaxSmem && need > smem) smem = need;
+    }
+    smemBytes = smem;
+    if (!dDesc) PD_CUDA(cudaMalloc(&dDesc, sizeof(pdg::InstanceDev) * inst.size()));
+    PD_CUDA(cudaMemcpy(dDesc, desc.data(), sizeof(pdg::InstanceDev) * desc.size(), cudaMemcpyHostToDevice));
+    return PD_OK;
+  }
+
+  // Copies device positions / velocities of every instance back into the host scenes.
+  int pullState() {
+    PD_CUDA(cudaStreamSynchronize(stream));
+    for (auto& I : inst) {
+      PD_CUDA(cudaMemcpy(I.scene.x.data(), dArena + I.oX, 24 * I.scene.n, cudaMemcpyDeviceToHost));
+      PD_CUDA(cudaMemcpy(I.scene.v.data(), dArena + I.oV, 24 * I.scene.n, cudaMemcpyDeviceToHost));
+    }
+    return PD_OK;
+  }
+};
+
+// ------------------------------------------------------------------------------ solver handle
+struct pd_solver {
+  int32_t n3 = 0;           // size of the 3n system
+  bool analyzedFlag = false;
+  bool ready = false;
+  std::vector<int32_t> pattern_cp, pattern_ri;
+  pdg::ScalarMatrix A;
+  pdg::Factor F;
+  std::vector<int32_t> perm;
+  uint8_t* dArena = nullptr;
+  pdg::InstanceDev* dDesc = nullptr;
+  double* dB = nullptr;
+  double* dX = nullptr;
+  cudaStream_t stream = nullptr;
+  pd_solver_stats stats{};
+  ~pd_solver() {
+    if (dArena) cudaFree(dArena);
+    if (dDesc) cudaFree(dDesc);
+    if (dB) cudaFree(dB);  // dX points into the same allocation
+  }
+};
+
+namespace {
+
+// Extracts the scalar matrix Ã from a 3n × 3n CSC matrix with L = Ã ⊗ I₃; returns "" on success.
+std::string scalarFromBlocks(int32_t n3, const int32_t* cp, const int32_t* ri, const double* val,
+                             pdg::ScalarMatrix& A) {
+  if (n3 <= 0 || n3 % 3 != 0) return "dimension is not a multiple of 3";
+  const int n = n3 / 3;
+  // collect entries (r, c, v) of component 0 and check the other components mirror them
+  std::vector<std::vector<std::pair<int, double>>> rows(n);
+  std::vector<std::vector<std::pair<int, double>>> comp[3];
+  for (int k = 0; k < 3; ++k) comp[k].assign(n, {});
+  for (int c = 0; c < n3; ++c)
+    for (int p = cp[c]; p < cp[c + 1]; ++p) {
+      const int r = ri[p];
+      if (r < 0 || r >= n3) return "row index out of range";
+      if (r % 3 != c % 3) return "matrix couples different x/y/z components";
+      comp[c % 3][r / 3].push_back({c / 3, val ? val[p] : 0.0});
+    }
+  for (int k = 0; k < 3; ++k)
+    for (auto& row : comp[k]) std::sort(row.begin(), row.end(), [](auto& a, auto& b) { return a.first < b.first; });
+  for (int r = 0; r < n; ++r)
+    for (int k = 1; k < 3; ++k) {
+      if (comp[k][r].size() != comp[0][r].size()) return "components have different sparsity";
+      for (size_t t = 0; t < comp[0][r].size(); ++t) {
+        if (comp[k][r][t].first != comp[0][r][t].first) return "components have different sparsity";
+        if (val && std::memcmp(&comp[k][r][t].second, &comp[0][r][t].second, sizeof(double)) != 0)
+          return "components have different values (not a scalar times I3 per block)";
+      }
+    }
+  // symmetrize the pattern from the lower triangle (Eigen's selfadjointView<Lower>)
+  std::vector<std::vector<std::pair<int, double>>> sym(n);
+  for (int r = 0; r < n; ++r)
+    for (auto& e : comp[0][r])
+      if (e.first <= r) {
+        sym[r].push_back({e.first, e.second});
+        if (e.first != r) sym[e.first].push_back({r, e.second});
+      }
+  A.n = n;
+  A.rowptr.assign(n + 1, 0);
+  A.col.clear();
+  A.val.clear();
+  for (int r = 0; r < n; ++r) {
+    std::sort(sym[r].begin(), sym[r].end(), [](auto& a, auto& b) { return a.first < b.first; });
+    for (auto& e : sym[r]) {
+      A.col.push_back(e.first);
+      A.val.push_back(e.second);
+    }
+    A.rowptr[r + 1] = static_cast<int32_t>(A.col.size());
+  }
+  return {};
+}
+
+// Minimum-degree ordering of a scalar pattern (ties → lower index); used when no geometry exists.
+std::vector<int32_t> minimumDegreeOrder(const pdg::ScalarMatrix& A) {
+  const int n = A.n;
+  std::vector<std::vector<int>> adj(n);
+  for (int r = 0; r < n; ++r)
+    for (int p = A.rowptr[r]; p < A.rowptr[r + 1]; ++p)
+      if (A.col[p] != r) adj[r].push_back(A.col[p]);
+  for (auto& a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  std::vector<std::pair<int, int>> heap;
+  std::vector<int> deg(n);
+  std::vector<uint8_t> done(n, 0);
+  for (int v = 0; v < n; ++v) deg[v] = static_cast<int>(adj[v].size());
+  std::vector<int32_t> order;
+  std::vector<int> merged;
+  auto better = [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; };
+  for (int step = 0; step < n; ++step) {
+    int best = -1;
+    for (int v = 0; v < n; ++v)
+      if (!done[v] && (best < 0 || better(v, best))) best = v;
+    done[best] = 1;
+    order.push_back(best);
+    const std::vector<int> nb = adj[best];
+    for (int u : nb) {
+      merged.clear();
+      std::set_union(adj[u].begin(), adj[u].end(), nb.begin(), nb.end(), std::back_inserter(merged));
+      adj[u].clear();
+      for (int w : merged)
+        if (w != u && w != best && !done[w]) adj[u].push_back(w);
+      deg[u] = static_cast<int>(adj[u].size());
+    }
+    adj[best].clear();
+  }
+  return order;
+}
+
+}  // namespace
+
+// ====================================================================================== C API
+extern "C" {
+
+const char* pd_last_error(void) { return g_lastError.c_str(); }
+
+void pd_scene_config_default(pd_scene_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->dt = 1.0 / 120.0;
+  c->substeps_per_frame = 2;
+  c->gravity[1] = -9.81;
+  c->stiffness = 2.3e3;
+  c->density = 1.0;
+  c->velocity_damping = 0.02;
+  c->max_iterations = 10;
+  c->rel_tolerance = 1.0e-3;
+  c->abs_tolerance = 1.0e-12;
+  c->residual_tolerance = 1.0e-3;
+  c->grid_nx = 40;
+  c->grid_ny = 40;
+  c->grid_spacing = 0.025;
+  c->bend_stride = 1;
+  c->total_mass = 1.0;
+  c->precision = PD_PRECISION_FP64_EXACT;
+}
+
+int pd_grid_counts(const pd_scene_config* cfg, int32_t* nv, int32_t* ne, int32_t* nb) {
+  if (!cfg || !nv || !ne || !nb) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  int a, b, c;
+  if (!pdg::gridCounts(gridSpecOf(*cfg), &a, &b, &c)) return fail(PD_ERR_INVALID_ARGUMENT, "grid needs nx, ny >= 2");
+  *nv = a;
+  *ne = b;
+  *nb = c;
+  return PD_OK;
+}
+
+int pd_make_grid(const pd_scene_config* cfg, double* pos, double* mass, uint8_t* pinned, int32_t* edges,
+                 double* rest, double* k, int32_t* bends, double* bk) {
+  if (!cfg || !pos || !mass || !pinned || !edges || !rest || !k) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  pdg::Scene s;
+  if (!pdg::makeGrid(gridSpecOf(*cfg), s)) return fail(PD_ERR_INVALID_ARGUMENT, "grid needs nx, ny >= 2");
+  if (!s.bends.empty() && (!bends || !bk)) return fail(PD_ERR_INVALID_ARGUMENT, "bend arrays are null");
+  std::memcpy(pos, s.x.data(), s.x.size() * sizeof(double));
+  std::memcpy(mass, s.m.data(), s.m.size() * sizeof(double));
+  std::memcpy(pinned, s.pinned.data(), s.pinned.size());
+  for (size_t e = 0; e < s.edges.size(); ++e) {
+    edges[2 * e] = s.edges[e].a;
+    edges[2 * e + 1] = s.edges[e].b;
+    rest[e] = s.edges[e].rest;
+    k[e] = s.edges[e].k;
+  }
+  for (size_t b = 0; b < s.bends.size(); ++b) {
+    bends[3 * b] = s.bends[b].a;
+    bends[3 * b + 1] = s.bends[b].b;
+    bends[3 * b + 2] = s.bends[b].c;
+    bk[b] = s.bends[b].k;
+  }
+  return PD_OK;
+}
+
+// ---------------------------------------------------------------------------------- sim
+static int sceneFromMesh(const pd_mesh& m, pdg::Scene& s) {
+  if (m.n_vertices <= 0 || !m.positions || !m.masses || !m.pinned)
+    return fail(PD_ERR_INVALID_ARGUMENT, "mesh needs vertices, positions, masses and pin flags");
+  if (m.n_edges < 0 || m.n_bends < 0) return fail(PD_ERR_INVALID_ARGUMENT, "negative edge or bend count");
+  if (m.n_edges > 0 && (!m.edges || !m.edge_rest || !m.edge_stiffness))
+    return fail(PD_ERR_INVALID_ARGUMENT, "edge arrays are null");
+  if (m.n_bends > 0 && (!m.bends || !m.bend_stiffness)) return fail(PD_ERR_INVALID_ARGUMENT, "bend arrays are null");
+  const size_t n = m.n_vertices;
+  s = pdg::Scene{};
+  s.n = m.n_vertices;
+  s.x.assign(m.positions, m.positions + 3 * n);
+  if (m.velocities) s.v.assign(m.velocities, m.velocities + 3 * n);
+  else s.v.assign(3 * n, 0.0);
+  s.m.assign(m.masses, m.masses + n);
+  s.pinned.assign(m.pinned, m.pinned + n);
+  for (auto& p : s.pinned) p = p ? 1 : 0;
+  if (m.pin_positions) s.q.assign(m.pin_positions, m.pin_positions + 3 * n);
+  else s.q = s.x;
+  for (int e = 0; e < m.n_edges; ++e)
+    s.edges.push_back(pdg::Edge{m.edges[2 * e], m.edges[2 * e + 1], m.edge_rest[e], m.edge_stiffness[e]});
+  for (int b = 0; b < m.n_bends; ++b)
+    s.bends.push_back(pdg::Bend{m.bends[3 * b], m.bends[3 * b + 1], m.bends[3 * b + 2], m.bend_stiffness[b]});
+  return PD_OK;
+}
+
+int pd_sim_create_batch(int32_t count, const pd_mesh* meshes, const pd_scene_config* cfgs, pd_sim** out) {
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (count <= 0 || !meshes || !cfgs) return fail(PD_ERR_INVALID_ARGUMENT, "empty batch");
+  auto sim = std::make_unique<pd_sim>();
+  sim->inst.resize(count);
+  for (int i = 0; i < count; ++i) {
+    Instance& I = sim->inst[i];
+    I.cfg = cfgs[i];
+    int rc = sceneFromMesh(meshes[i], I.scene);
+    if (rc != PD_OK) return rc;
+    std::string err = pdg::validateScene(I.scene);
+    if (!err.empty()) return fail(PD_ERR_INVALID_ARGUMENT, "instance " + std::to_string(i) + ": " + err);
+    pdg::buildTopology(I.scene, I.topo);
+    err = prepare(I, true);
+    if (!err.empty()) {
+      return fail(prepareCode(err), "instance " + std::to_string(i) + ": " + err);
+    }
+  }
+  const int rc = sim->upload(1);
+  if (rc != PD_OK) return rc;
+  *out = sim.release();
+  return PD_OK;
+}
+
+int pd_sim_create(const pd_mesh* mesh, const pd_scene_config* cfg, pd_sim** out) {
+  if (!mesh || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  return pd_sim_create_batch(1, mesh, cfg, out);
+}
+
+int pd_sim_destroy(pd_sim* s) {
+  delete s;
+  return PD_OK;
+}
+
+int pd_sim_instance_count(const pd_sim* s) { return s ? static_cast<int>(s->inst.size()) : 0; }
+
+int pd_sim_set_stream(pd_sim* s, void* stream) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  s->stream = static_cast<cudaStream_t>(stream);
+  return PD_OK;
+}
+
+int pd_sim_step(pd_sim* s, int32_t substeps) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (substeps < 0) return fail(PD_ERR_INVALID_ARGUMENT, "substeps must be >= 0");
+  if (substeps == 0) return PD_OK;
+  if (substeps > s->logCapacity) {
+    PD_CUDA(cudaStreamSynchronize(s->stream));
+    const int rc = s->ensureLogs(substeps);
+    if (rc != PD_OK) return rc;
+  }
+  const int rc = pdg::launchSubstepExact(s->dDesc, static_cast<int>(s->inst.size()), substeps, s->smemBytes, s->stream);
+  if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
+  s->lastSubsteps = substeps;
+  return PD_OK;
+}
+
+int pd_sim_synchronize(pd_sim* s) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  return PD_OK;
+}
+
+static int checkInstance(pd_sim* s, int32_t i) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (i < 0 || i >= static_cast<int>(s->inst.size())) return fail(PD_ERR_INVALID_ARGUMENT, "instance index out of range");
+  return PD_OK;
+}
+
+int pd_sim_get_state(pd_sim* s, int32_t i, double* x, double* v) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  const Instance& I = s->inst[i];
+  const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
+  if (x) PD_CUDA(cudaMemcpyAsync(x, s->dArena + I.oX, bytes, cudaMemcpyDeviceToHost, s->stream));
+  if (v) PD_CUDA(cudaMemcpyAsync(v, s->dArena + I.oV, bytes, cudaMemcpyDeviceToHost, s->stream));
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  return PD_OK;
+}
+
+int pd_sim_set_state(pd_sim* s, int32_t i, const double* x, const double* v) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  Instance& I = s->inst[i];
+  const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
+  if (x) {
+    for (size_t k = 0; k < 3 * static_cast<size_t>(I.scene.n); ++k)
+      if (!std::isfinite(x[k])) return fail(PD_ERR_INVALID_ARGUMENT, "positions contain a non-finite value");
+    PD_CUDA(cudaMemcpyAsync(s->dArena + I.oX, x, bytes, cudaMemcpyHostToDevice, s->stream));
+  }
+  if (v) PD_CUDA(cudaMemcpyAsync(s->dArena + I.oV, v, bytes, cudaMemcpyHostToDevice, s->stream));
+  return PD_OK;
+}
+
+int pd_sim_device_state(pd_sim* s, int32_t i, double** x, double** v) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (x) *x = reinterpret_cast<double*>(s->dArena + s->inst[i].oX);
+  if (v) *v = reinterpret_cast<double*>(s->dArena + s->inst[i].oV);
+  return PD_OK;
+}
+
+// Rebuilds host preparation of instance i after a change and re-uploads the handle.
+static int rebuild(pd_sim* s, int i, bool reanalyze) {
+  int rc = s->pullState();
+  if (rc) return rc;
+  Instance& I = s->inst[i];
+  const std::string err = prepare(I, reanalyze);
+  if (!err.empty()) return fail(prepareCode(err), err);
+  return s->upload(s->logCapacity > 0 ? s->logCapacity : 1);
+}
+
+int pd_sim_set_pin_positions(pd_sim* s, int32_t i, const double* q) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!q) return fail(PD_ERR_INVALID_ARGUMENT, "null pin positions");
+  Instance& I = s->inst[i];
+  I.scene.q.assign(q, q + 3 * static_cast<size_t>(I.scene.n));
+  pdg::assembleBendingRhs(I.scene, I.bendRhs);
+  PD_CUDA(cudaMemcpyAsync(s->dArena + I.oQ, I.scene.q.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
+  PD_CUDA(cudaMemcpyAsync(s->dArena + I.oBend, I.bendRhs.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  return PD_OK;
+}
+
+int pd_sim_set_edge_stiffness(pd_sim* s, int32_t i, const double* k) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!k) return fail(PD_ERR_INVALID_ARGUMENT, "null stiffness");
+  Instance& I = s->inst[i];
+  for (size_t e = 0; e < I.scene.edges.size(); ++e) I.scene.edges[e].k = k[e];
+  if (pdg::computeStamp(I.scene, I.cfg.dt).k == I.stamp.k) return PD_OK;  // L unchanged
+  return rebuild(s, i, false);
+}
+
+int pd_sim_set_pinned(pd_sim* s, int32_t i, const uint8_t* pinned, const double* q) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!pinned) return fail(PD_ERR_INVALID_ARGUMENT, "null pin mask");
+  rc = s->pullState();
+  if (rc) return rc;
+  Instance& I = s->inst[i];
+  for (int v = 0; v < I.scene.n; ++v) I.scene.pinned[v] = pinned[v] ? 1 : 0;
+  if (q) I.scene.q.assign(q, q + 3 * static_cast<size_t>(I.scene.n));
+  else
+    for (int v = 0; v < I.scene.n; ++v)
+      if (I.scene.pinned[v])
+        for (int c = 0; c < 3; ++c) I.scene.q[3 * v + c] = I.scene.x[3 * v + c];
+  const pdg::Stamp now = pdg::computeStamp(I.scene, I.cfg.dt);
+  if (now.pin == I.stamp.pin && now.structure == I.stamp.structure) {
+    pdg::assembleBendingRhs(I.scene, I.bendRhs);
+    return s->upload(s->logCapacity);
+  }
+  return rebuild(s, i, now.structure != I.stamp.structure);
+}
+
+int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
+  if (!s || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  if (!(cfg->dt > 0.0) || cfg->max_iterations < 0) return fail(PD_ERR_INVALID_ARGUMENT, "invalid dt or iteration count");
+  if (cfg->precision != PD_PRECISION_FP64_EXACT) return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
+  bool refactor = false;
+  for (auto& I : s->inst) {
+    refactor = refactor || (std::memcmp(&I.cfg.dt, &cfg->dt, sizeof(double)) != 0);
+    I.cfg = *cfg;
+  }
+  if (refactor) {
+    int rc = s->pullState();
+    if (rc) return rc;
+    for (auto& I : s->inst) {
+      const std::string err = prepare(I, false);
+      if (!err.empty()) return fail(PD_ERR_FACTORIZATION, err);
+    }
+    return s->upload(s->logCapacity);
+  }
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  return s->writeDescriptors();
+}
+
+int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
+  const Instance& I = s->inst[i];
+  out->n_vertices = I.scene.n;
+  out->n_edges = static_cast<int32_t>(I.scene.edges.size());
+  out->n_bends = static_cast<int32_t>(I.scene.bends.size());
+  out->color_count = I.topo.colorCount;
+  out->matrix_nnz = static_cast<int64_t>(I.L.val.size());
+  out->factor_nnz = static_cast<int64_t>(I.F.colval.size());
+  out->forward_levels = static_cast<int32_t>(I.F.fwdLevelPtr.size()) - 1;
+  out->backward_levels = static_cast<int32_t>(I.F.bwdLevelPtr.size()) - 1;
+  out->factorize_count = I.factorizeCount;
+  out->analyze_count = I.analyzeCount;
+  out->device_bytes = static_cast<int64_t>(I.bytes);
+  return PD_OK;
+}
+
+int pd_sim_get_stats(pd_sim* s, int32_t i, pd_sim_stats* out) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
+  const Instance& I = s->inst[i];
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  int32_t ints[3];
+  PD_CUDA(cudaMemcpy(&out->last_residual, s->dArena + I.oLastRes, sizeof(double), cudaMemcpyDeviceToHost));
+  PD_CUDA(cudaMemcpy(&ints[0], s->dArena + I.oIters, 4, cudaMemcpyDeviceToHost));
+  PD_CUDA(cudaMemcpy(&ints[1], s->dArena + I.oConv, 4, cudaMemcpyDeviceToHost));
+  PD_CUDA(cudaMemcpy(&ints[2], s->dArena + I.oEarly, 4, cudaMemcpyDeviceToHost));
+  out->iterations_used = ints[0];
+  out->converged = ints[1];
+  out->early_exit_count = ints[2];
+  return PD_OK;
+}
+
+int pd_sim_iteration_log(pd_sim* s, int32_t i, int32_t* iters, uint8_t* conv, int32_t count) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (count < 0 || count > s->lastSubsteps) return fail(PD_ERR_INVALID_ARGUMENT, "count exceeds the last step's substeps");
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (iters) PD_CUDA(cudaMemcpy(iters, s->dIterLog + static_cast<size_t>(i) * s->logCapacity, 4 * count, cudaMemcpyDeviceToHost));
+  if (conv) PD_CUDA(cudaMemcpy(conv, s->dConvLog + static_cast<size_t>(i) * s->logCapacity, count, cudaMemcpyDeviceToHost));
+  return PD_OK;
+}
+
+int pd_sim_get_factor(pd_sim* s, int32_t i, int32_t* perm, int32_t* colptr, int32_t* rowidx, double* val,
+                      double* dinv, int64_t* nnz) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  const pdg::Factor& F = s->inst[i].F;
+  if (nnz) *nnz = static_cast<int64_t>(F.colval.size());
+  if (perm) std::memcpy(perm, F.perm.data(), F.perm.size() * 4);
+  if (colptr) std::memcpy(colptr, F.colptr.data(), F.colptr.size() * 4);
+  if (rowidx) std::memcpy(rowidx, F.rowidx.data(), F.rowidx.size() * 4);
+  if (val) std::memcpy(val, F.colval.data(), F.colval.size() * 8);
+  if (dinv) std::memcpy(dinv, F.dinv.data(), F.dinv.size() * 8);
+  return PD_OK;
+}
+
+int pd_sim_solve(pd_sim* s, int32_t i, const double* b, double* x) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!b || !x) return fail(PD_ERR_INVALID_ARGUMENT, "null vector");
+  const Instance& I = s->inst[i];
+  const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
+  double* dB = nullptr;
+  PD_CUDA(cudaMalloc(&dB, 2 * bytes));
+  double* dX = dB + 3 * static_cast<size_t>(I.scene.n);
+  PD_CUDA(cudaMemcpyAsync(dB, b, bytes, cudaMemcpyHostToDevice, s->stream));
+  const int smem = (24 * I.scene.n <= kMaxSmem) ? 24 * I.scene.n : 0;
+  const int lrc = pdg::launchSolveExact(s->dDesc + i, dB, dX, smem, s->stream);
+  if (lrc != 0) {
+    cudaFree(dB);
+    return cudaFail(static_cast<cudaError_t>(lrc), "solve launch");
+  }
+  PD_CUDA(cudaMemcpyAsync(x, dX, bytes, cudaMemcpyDeviceToHost, s->stream));
+  PD_CUDA(cudaStreamSynchronize(s->stream));
+  PD_CUDA(cudaFree(dB));
+  return PD_OK;
+}
+
+int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* perm, int32_t* colptr,
+                    int32_t* rowidx, double* val, double* dinv, int64_t* nnz, pd_sim_info* info) {
+  if (!mesh || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  Instance I;
+  I.cfg = *cfg;
+  int rc = sceneFromMesh(*mesh, I.scene);
+  if (rc) return rc;
+  std::string err = pdg::validateScene(I.scene);
+  if (!err.empty()) return fail(PD_ERR_INVALID_ARGUMENT, err);
+  pdg::buildTopology(I.scene, I.topo);
+  err = prepare(I, true);
+  if (!err.empty()) return fail(prepareCode(err), err);
+  const pdg::Factor& F = I.F;
+  if (nnz) *nnz = static_cast<int64_t>(F.colval.size());
+  if (perm) std::memcpy(perm, F.perm.data(), F.perm.size() * 4);
+  if (colptr) std::memcpy(colptr, F.colptr.data(), F.colptr.size() * 4);
+  if (rowidx) std::memcpy(rowidx, F.rowidx.data(), F.rowidx.size() * 4);
+  if (val) std::memcpy(val, F.colval.data(), F.colval.size() * 8);
+  if (dinv) std::memcpy(dinv, F.dinv.data(), F.dinv.size() * 8);
+  if (info) {
+    Arena A;
+    layout(I, A);
+    info->n_vertices = I.scene.n;
+    info->n_edges = static_cast<int32_t>(I.scene.edges.size());
+    info->n_bends = static_cast<int32_t>(I.scene.bends.size());
+    info->color_count = I.topo.colorCount;
+    info->matrix_nnz = static_cast<int64_t>(I.L.val.size());
+    info->factor_nnz = static_cast<int64_t>(F.colval.size());
+    info->forward_levels = static_cast<int32_t>(F.fwdLevelPtr.size()) - 1;
+    info->backward_levels = static_cast<int32_t>(F.bwdLevelPtr.size()) - 1;
+    info->factorize_count = I.factorizeCount;
+    info->analyze_count = I.analyzeCount;
+    info->device_bytes = static_cast<int64_t>(I.bytes);
+  }
+  return PD_OK;
+}
+
+int pd_scene_coloring(const pd_mesh* mesh, uint32_t* color_of, int32_t* colors) {
+  if (!mesh) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  pdg::Scene s;
+  int rc = sceneFromMesh(*mesh, s);
+  if (rc) return rc;
+  const std::string err = pdg::validateScene(s);
+  if (!err.empty()) return fail(PD_ERR_INVALID_ARGUMENT, err);
+  pdg::Topology t;
+  pdg::buildTopology(s, t);
+  if (color_of) std::memcpy(color_of, t.colorOf.data(), t.colorOf.size() * 4);
+  if (colors) *colors = t.colorCount;
+  return PD_OK;
+}
+
+// ------------------------------------------------------------------------------- solver
+int pd_solver_create(pd_solver** out) {
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "out is null");
+  *out = new pd_solver();
+  return PD_OK;
+}
+
+int pd_solver_destroy(pd_solver* s) {
+  delete s;
+  return PD_OK;
+}
+
+int pd_solver_analyze(pd_solver* s, int32_t n, const int32_t* cp, const int32_t* ri) {
+  if (!s || !cp || !ri || n <= 0) return fail(PD_ERR_INVALID_ARGUMENT, "invalid pattern");
+  const auto t0 = Clock::now();
+  pdg::ScalarMatrix A;
+  const std::string err = scalarFromBlocks(n, cp, ri, nullptr, A);
+  if (!err.empty()) return fail(PD_ERR_UNSUPPORTED, err);
+  s->n3 = n;
+  s->pattern_cp.assign(cp, cp + n + 1);
+  s->pattern_ri.assign(ri, ri + cp[n]);
+  s->perm = minimumDegreeOrder(A);
+  s->analyzedFlag = true;
+  s->ready = false;
+  s->stats.analyze_calls += 1;
+  s->stats.last_analyze_seconds = secondsSince(t0);
+  s->stats.nnz = cp[n];
+  return PD_OK;
+}
+
+int pd_solver_analyzed(const pd_solver* s) { return (s && s->analyzedFlag) ? 1 : 0; }
+
+int pd_solver_factorize(pd_solver* s, int32_t n, const int32_t* cp, const int32_t* ri, const double* val) {
+  if (!s || !cp || !ri || !val) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  if (!s->analyzedFlag) return fail(PD_ERR_STATE, "factorize before analyze");
+  if (n != s->n3 || cp[n] != s->pattern_cp[n] || std::memcmp(cp, s->pattern_cp.data(), 4 * (n + 1)) != 0 ||
+      std::memcmp(ri, s->pattern_ri.data(), 4 * static_cast<size_t>(cp[n])) != 0)
+    return fail(PD_ERR_STATE, "structure differs from the analysed pattern");
+  const auto t0 = Clock::now();
+  s->ready = false;
+  s->stats.factorize_calls += 1;
+  std::string err = scalarFromBlocks(n, cp, ri, val, s->A);
+  if (!err.empty()) return fail(PD_ERR_UNSUPPORTED, err);
+  if (!pdg::factorize(s->A, s->perm, s->F, &err)) return fail(PD_ERR_FACTORIZATION, err);
+  // upload the factor as a solve-only instance
+  Arena A;
+  const size_t m = s->A.n;
+  const size_t oIperm = A.add(s->F.iperm), oLrp = A.add(s->F.rowptr), oLci = A.add(s->F.colidx),
+               oLrv = A.add(s->F.rowval), oLcp = A.add(s->F.colptr), oLri = A.add(s->F.rowidx),
+               oLcv = A.add(s->F.colval), oDinv = A.add(s->F.dinv), oFp = A.add(s->F.fwdLevelPtr),
+               oFr = A.add(s->F.fwdRows), oBp = A.add(s->F.bwdLevelPtr), oBr = A.add(s->F.bwdRows),
+               oW = A.zeros(24 * m);
+  if (s->dArena) cudaFree(s->dArena);
+  if (s->dB) cudaFree(s->dB);
+  s->dArena = nullptr;
+  s->dB = nullptr;
+  PD_CUDA(cudaMalloc(&s->dArena, A.host.size()));
+  PD_CUDA(cudaMemcpy(s->dArena, A.host.data(), A.host.size(), cudaMemcpyHostToDevice));
+  PD_CUDA(cudaMalloc(&s->dB, 2 * 24 * m));
+  s->dX = s->dB + 3 * m;
+  pdg::InstanceDev d{};
+  d.n = static_cast<int32_t>(m);
+  d.nlevF = static_cast<int32_t>(s->F.fwdLevelPtr.size()) - 1;
+  d.nlevB = static_cast<int32_t>(s->F.bwdLevelPtr.size()) - 1;
+  auto P = [&](size_t off) { return s->dArena + off; };
+  d.iperm = reinterpret_cast<const int32_t*>(P(oIperm));
+  d.Lrp = reinterpret_cast<const int32_t*>(P(oLrp));
+  d.Lci = reinterpret_cast<const int32_t*>(P(oLci));
+  d.Lrv = reinterpret_cast<const double*>(P(oLrv));
+  d.Lcp = reinterpret_cast<const int32_t*>(P(oLcp));
+  d.Lri = reinterpret_cast<const int32_t*>(P(oLri));
+  d.Lcv = reinterpret_cast<const double*>(P(oLcv));
+  d.dinv = reinterpret_cast<const double*>(P(oDinv));
+  d.fwdPtr = reinterpret_cast<const int32_t*>(P(oFp));
+  d.fwdRows = reinterpret_cast<const int32_t*>(P(oFr));
+  d.bwdPtr = reinterpret_cast<const int32_t*>(P(oBp));
+  d.bwdRows = reinterpret_cast<const int32_t*>(P(oBr));
+  d.w = reinterpret_cast<double*>(P(oW));
+  if (!s->dDesc) PD_CUDA(cudaMalloc(&s->dDesc, sizeof(pdg::InstanceDev)));
+  PD_CUDA(cudaMemcpy(s->dDesc, &d, sizeof(d), cudaMemcpyHostToDevice));
+  s->ready = true;
+  s->stats.last_factorize_seconds = secondsSince(t0);
+  s->stats.total_factorize_seconds += s->stats.last_factorize_seconds;
+  s->stats.nnz = cp[n];
+  s->stats.factor_nnz = static_cast<int64_t>(s->F.colval.size());
+  return PD_OK;
+}
+
+static int solverSolve(pd_solver* s, const double* b, double* x, int component) {
+  if (!s || !b || !x) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  if (!s->ready) return fail(PD_ERR_STATE, "solve before a successful factorize");
+  const size_t m = s->A.n, bytes = 24 * m;
+  PD_CUDA(cudaMemcpyAsync(s->dB, b, bytes, cudaMemcpyHostToDevice, s->stream));
+  const int smem = (24 * static_cast<int>(m) <= kMaxSmem) ? 24 * static_cast<int>(m) : 0;
+  const int rc = pdg::launchSolveExact(s->dDesc, s->dB, s->dX, smem, s->stream);
+  if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "solve launch");
+  if (component < 0) {
+    PD_CUDA(cudaMemcpyAsync(x, s->dX, bytes, cudaMemcpyDeviceToHost, s->stream));
+    PD_CUDA(cudaStreamSynchronize(s->stream));
+  } else {
+    std::vector<double> tmp(3 * m);
+    PD_CUDA(cudaMemcpyAsync(tmp.data(), s->dX, bytes, cudaMemcpyDeviceToHost, s->stream));
+    PD_CUDA(cudaStreamSynchronize(s->stream));
+    for (size_t v = 0; v < m; ++v) x[3 * v + component] = tmp[3 * v + component];
+  }
+  return PD_OK;
+}
+
+int pd_solver_solve(pd_solver* s, const double* b, double* x) {
+  const auto t0 = Clock::now();
+  const int rc = solverSolve(s, b, x, -1);
+  if (rc == PD_OK) {
+    s->stats.solve_calls += 1;
+    s->stats.last_solve_seconds = secondsSince(t0);
+    s->stats.total_solve_seconds += s->stats.last_solve_seconds;
+  }
+  return rc;
+}
+
+int pd_solver_parallel_components(const pd_solver* s) { return (s && s->analyzedFlag) ? 3 : 1; }
+
+int pd_solver_solve_component(pd_solver* s, int32_t c, const double* b, double* x) {
+  if (c < 0 || c > 2) return fail(PD_ERR_INVALID_ARGUMENT, "component out of range");
+  return solverSolve(s, b, x, c);
+}
+
+int pd_solver_note_solve_stage(pd_solver* s, double seconds) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  s->stats.solve_calls += 1;
+  s->stats.last_solve_seconds = seconds;
+  s->stats.total_solve_seconds += seconds;
+  return PD_OK;
+}
+
+int pd_solver_stats_get(const pd_solver* s, pd_solver_stats* out) {
+  if (!s || !out) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = s->stats;
+  return PD_OK;
+}
+
+}  // extern "C"

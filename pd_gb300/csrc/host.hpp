@@ -1,0 +1,100 @@
+// host.hpp — host-side preparation of a cloth instance for the GPU substep.
+//
+// Everything here is one-time (or once-per-stamp-change) work that the reference does on the
+// CPU before its per-substep loop: topology (colouring and incidence CSRs), assembly of the
+// constant matrix L, a fill-reducing ordering, the LDLᵀ factorization and, new here, the
+// level schedules that let the GPU run the triangular solves in the reference's exact order.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace pdg {
+
+struct Edge {
+  int32_t a, b;
+  double rest, k;
+};
+struct Bend {
+  int32_t a, b, c;
+  double k;
+};
+
+// Raw scene of one cloth (positions etc. interleaved [x,y,z] per vertex).
+struct Scene {
+  int32_t n = 0;
+  std::vector<double> x, v, m, q;
+  std::vector<uint8_t> pinned;
+  std::vector<Edge> edges;
+  std::vector<Bend> bends;
+};
+
+// Topology shared by the scatter and residual gathers (core/mesh/ConstraintColoring.h:34-81).
+struct Topology {
+  int colorCount = 0;
+  std::vector<uint32_t> colorOf;
+  // vertex → incident edges in colour order (the reference's per-vertex scatter summation order)
+  std::vector<int32_t> sstart, sinc;  // sinc = edge << 1 | (vertex is endpoint b)
+  // vertex → incident edges in edge-index order (residual gather order, vertexEdges)
+  std::vector<int32_t> rstart, rinc;
+  // vertex → bend stencils in stencil order, with the stencil's (-k)·w_v factor
+  std::vector<int32_t> bstart, binc;
+  std::vector<double> bfac;
+};
+
+// Scalar matrix Ã (n×n, L = Ã ⊗ I₃) in CSR with sorted columns.
+struct ScalarMatrix {
+  int32_t n = 0;
+  std::vector<int32_t> rowptr, col;
+  std::vector<double> val;
+};
+
+// LDLᵀ factor of P·Ã·Pᵀ: perm[k] = vertex eliminated k-th; L strictly lower, unit diagonal.
+struct Factor {
+  int32_t n = 0;
+  std::vector<int32_t> perm, iperm;
+  std::vector<int32_t> colptr, rowidx;  // CSC, rows ascending (backward solve gathers columns)
+  std::vector<double> colval;
+  std::vector<int32_t> rowptr, colidx;  // CSR, columns ascending (forward solve gathers rows)
+  std::vector<double> rowval;
+  std::vector<double> d, dinv;
+  std::vector<int32_t> parent;          // elimination tree
+  // level schedules: rows grouped by dependency depth (forward: leaves first; backward: root first)
+  std::vector<int32_t> fwdLevelPtr, fwdRows, bwdLevelPtr, bwdRows;
+};
+
+void buildTopology(const Scene& s, Topology& t);
+void assembleMatrix(const Scene& s, double dt, ScalarMatrix& L);
+void assembleBendingRhs(const Scene& s, std::vector<double>& out);
+// Nested dissection by recursive coordinate bisection of the rest positions (vertex separators
+// taken from the graph of Ã), leaves in index order.
+std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int leafSize = 24);
+// Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
+bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
+void buildSchedules(Factor& f);
+
+// Regular-grid scene (Mesh::makeGrid, computeMassesFromEdges, addShearDiagonals,
+// addBendingStencils and the default pins of makeScene).
+struct GridSpec {
+  int nx = 40, ny = 40;
+  double spacing = 0.025, stiffness = 2.3e3, density = 1.0;
+  double shearStiffness = 0.0, bendStiffness = 0.0;
+  int bendSampling = 0, bendStride = 1;
+  int massMode = 0;  // 0 edge-lumped, 1 uniform totalMass
+  double totalMass = 1.0;
+  int pinMode = 0;   // 0 corners of row ny-1, 1 corners of row 0, 2 row ny-1, 3 corner (0,ny-1), 4 none
+};
+bool gridCounts(const GridSpec& g, int* nv, int* ne, int* nb);
+bool makeGrid(const GridSpec& g, Scene& s);
+
+// Hashes that decide refactorization (core/assemble/Assembler.cpp:29-92).
+struct Stamp {
+  uint64_t k = 0, m = 0, pin = 0, dt = 0, structure = 0;
+};
+Stamp computeStamp(const Scene& s, double dt);
+
+// Validation of raw inputs; returns an error message or empty.
+std::string validateScene(const Scene& s);
+
+}  // namespace pdg

@@ -1,0 +1,31 @@
+"""Shared helpers: build the oracle twin of a GPU scene (same arrays, same elimination order)."""
+import numpy as np
+
+from oracle import oracle as O
+
+
+def oracle_config(cfg, threads=0):
+    return O.Config(dt=cfg.dt, gravity=tuple(cfg.gravity), velocity_damping=cfg.velocity_damping,
+                    max_iterations=cfg.max_iterations, rel_tolerance=cfg.rel_tolerance,
+                    abs_tolerance=cfg.abs_tolerance, residual_tolerance=cfg.residual_tolerance,
+                    threads=threads)
+
+
+def oracle_twin(scene, cfg, perm=None, threads=0):
+    mesh = O.Mesh(positions=np.asarray(scene.positions, np.float64), masses=scene.masses,
+                  pinned=scene.pinned, edges=np.asarray(scene.edges, np.int32).reshape(-1, 2),
+                  edge_rest=scene.edge_rest, edge_k=scene.edge_stiffness,
+                  bends=np.asarray(scene.bends, np.int32).reshape(-1, 3), bend_k=scene.bend_stiffness,
+                  velocities=scene.velocities, pin_positions=scene.pin_positions)
+    return O.OracleSim(mesh, oracle_config(cfg, threads), perm=perm)
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.uint64)
+
+
+def max_rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.max(np.abs(b)), 1e-300)
+    return float(np.max(np.abs(a - b)) / scale)
