@@ -1,0 +1,327 @@
+"""Benchmark of the GB300 Projective Dynamics substep: PD substeps/s.
+
+A step is one PD substep (predict, K iterations, velocity update) of the workload's cloth(s).
+Default workload: the 40×40 cloth with distance, shear and bend constraints, 40 iterations and
+a 1e-3·|g| residual gate (``pd_gb300.workloads.cloth40_full``).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+Prints one JSON line. ``value`` times the substep kernel with its data resident in HBM (CUDA
+events on the simulator's stream, L2 flushed between timed steps); ``e2e`` times the same
+substeps through the C ABI with the state copied from pinned host memory and read back every
+step. ``--impl reference`` times the CPU oracle (the reference algorithm restated) on all host
+cores instead. Under torchrun each rank steps its own cloth(s) (replicas; no collective on the
+data path) and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PD substeps/s (1 cloth & 512-batch) vs plain FP64 GPU at 1e-5 pos err; grads/s"
+UNIT = "substeps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--workload", default="cloth40_full")
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch-count", type=int, default=512)
+    p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name, batch_count):
+    from pd_gb300 import workloads as W
+    if name == "batch":
+        scenes, cfgs, sub = W.batch(count=batch_count)
+        return scenes, cfgs, sub
+    scenes, cfg, sub = W.WORKLOADS[name]()
+    return scenes, [cfg] * len(scenes), sub
+
+
+def describe_workload(name, scenes, cfgs):
+    c = cfgs[0]
+    n = sum(s.n for s in scenes)
+    e = sum(int(s.edges.shape[0]) for s in scenes)
+    b = sum(int(np.asarray(s.bends).reshape(-1, 3).shape[0]) for s in scenes)
+    return {"workload": name, "instances": len(scenes), "vertices": n, "constraints": e, "bend_stencils": b,
+            "iterations": c.max_iterations, "residual_tolerance": c.residual_tolerance, "dt": c.dt,
+            "precision": "fp64-reference-order"}
+
+
+# --------------------------------------------------------------------------------- roofline
+def algorithmic_bytes(scene, factor_nnz, iterations):
+    """Bytes one substep must move (the per-unit formula stated in the design doc)."""
+    n = scene.n
+    E = int(scene.edges.shape[0])
+    S = int(np.asarray(scene.bends).reshape(-1, 3).shape[0])
+    F = factor_nnz
+    b_ps = 24 * n * 3 + (24 * n if S else 0) + 24 * E + 8 * E + 4 * (n + 1) + n
+    b_solve = 2 * F * (8 + 4) + 8 * n + 8 * (n + 1) + 2 * 24 * n + 8 * n
+    b_res = 24 * n * 5 + 8 * n + 32 * E + 4 * (n + 1) + ((3 * S * 12 + 24 * S) if S else 0)
+    return iterations * (b_ps + b_solve + b_res) + 96 * n + 72 * n
+
+
+def fp64_ops(scene, factor_nnz, iterations):
+    """FP64 operations one substep issues (sqrt and divide counted as one each)."""
+    n = scene.n
+    E = int(scene.edges.shape[0])
+    S = int(np.asarray(scene.bends).reshape(-1, 3).shape[0])
+    F = factor_nnz
+    edge = E * (3 + 5 + 1 + 1 + 3 + 3 + 6)        # rel, dot, sqrt, div, d, κd, residual term
+    gather = 2 * E * 3 + n * 3                     # scatter sums
+    solve = 3 * (2 * F * 2 + n)                     # mul + sub per factor entry, both sweeps
+    res = 2 * E * 3 + 3 * S * 9 + n * 16           # residual sums, bend force, inertia + norm
+    return iterations * (edge + gather + solve + res) + edge + n * 12
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(scenes, cfgs, substeps_total, max_seconds, threads=0):
+    """The oracle on the host cores: substeps/s over a bounded sample of the same workload."""
+    from oracle import oracle as O  # noqa: F401  (checker / baseline only)
+    from tests.helpers import oracle_twin
+    ncores = threads or os.cpu_count()
+    done = 0
+    t_total = 0.0
+    sims = [oracle_twin(s, c, threads=ncores) for s, c in zip(scenes, cfgs)]
+    sims[0].step(1)  # factorization happens in the first step; exclude it
+    for k in range(substeps_total):
+        t0 = time.perf_counter()
+        for s in sims:
+            s.step(1)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > max_seconds:
+            break
+    return {"value": done / t_total, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"{done} consecutive substeps of the workload ({len(sims)} cloth(s)) on the CPU oracle, "
+                      f"{t_total:.1f} s, OpenMP {ncores} threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    scenes, cfgs, sub = workload(args.workload, args.batch_count)
+    from tests.helpers import oracle_twin
+    ncores = os.cpu_count()
+    sims = [oracle_twin(s, c, threads=ncores) for s, c in zip(scenes, cfgs)]
+    for _ in range(args.warmup):
+        for s in sims:
+            s.step(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in sims:
+            s.step(1)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": describe_workload(args.workload, scenes, cfgs), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": f"{args.steps} consecutive substeps after {args.warmup} warm-up substeps, "
+                                       f"CPU oracle (reference algorithm restated), OpenMP {ncores} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------ ours
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import pd_gb300 as P
+
+    scenes, cfgs, sub = workload(args.workload, args.batch_count)
+    sim = P.Simulator(scenes, cfgs)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- value: device-resident state, one launch per substep, L2 flushed between steps
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sim.step(1, sync=False)
+            flush.fill_(1.0)
+    barrier()
+    sampler = ClockSampler(local) if rank == 0 else None
+    t_wall = time.perf_counter()
+    iters_used = []
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            starts[k].record(stream)
+            sim.step(1, sync=False)
+            ends[k].record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall
+    clocks = sampler.stop() if sampler else None
+    for i in range(sim.count):
+        it, _ = sim.iteration_log(i)
+        iters_used.append(int(it[0]))
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    kernel_ms = ms / args.steps
+    t_local = torch.tensor([ms / 1e3], device="cuda", dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    t_max = float(t_local.item())
+    value = world * args.steps / t_max
+
+    # ---- e2e: through the C ABI, state copied from pinned host memory and read back every step
+    x0, v0 = sim.state(0)
+    host_x = torch.from_numpy(x0.copy()).pin_memory()
+    host_v = torch.from_numpy(v0.copy()).pin_memory()
+    hx, hv = host_x.numpy(), host_v.numpy()
+    n0 = scenes[0].n
+    h2d = d2h = 0
+    sim.set_stream(None)
+    for _ in range(args.warmup):
+        sim.set_state(0, hx, hv)
+        sim.step(1, sync=False)
+        sim.state(0)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.set_state(0, hx, hv)           # H2D from pinned memory: positions + velocities
+        sim.step(1, sync=False)
+        sim.state(0, out_x=hx, out_v=hv)   # D2H into pinned memory (waits for the step)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    h2d = d2h = 2 * 24 * n0
+    e_local = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(e_local, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * args.steps / float(e_local.item())
+
+    if rank == 0:
+        info = sim.info(0)
+        iters = max(1, iters_used[0])
+        per_launch_bytes = sum(algorithmic_bytes(s, sim.info(i)["factor_nnz"], iters_used[i])
+                               for i, s in enumerate(scenes))
+        ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
+        peak, peak_kind = read_peaks()
+        achieved = per_launch_bytes / (kernel_ms * 1e-3) / 1e9
+        fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU (profiles/)
+        fp64_achieved = ops / (kernel_ms * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(describe_workload(args.workload, scenes, cfgs),
+                               l2="flushed between timed substeps (256 MB device write outside the timed events)",
+                               parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                               factor_nnz=info["factor_nnz"], iterations_used=iters_used[0]),
+                "wall_s": t_wall,
+                "gpu_launches": args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                             "kernel": "substepExactKernel",
+                             "algorithmic_bytes_per_launch": per_launch_bytes},
+                "fp64": {"achieved_gops": fp64_achieved, "peak_gops": fp64_peak,
+                         "frac": fp64_achieved / fp64_peak, "ops_per_launch": ops},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "clocks": clocks}
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(scenes, cfgs, sub, args.cpu_sample_seconds)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -322,9 +322,13 @@ class Simulator:
     def set_stream(self, stream_ptr: int | None):
         _check(self._lib.pd_sim_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
-    def state(self, i: int = 0):
-        x = np.zeros((self.n[i], 3))
-        v = np.zeros((self.n[i], 3))
+    def state(self, i: int = 0, out_x=None, out_v=None):
+        """Positions and velocities of instance i (waits for queued work); optional out arrays."""
+        x = np.zeros((self.n[i], 3)) if out_x is None else out_x
+        v = np.zeros((self.n[i], 3)) if out_v is None else out_v
+        for a in (x, v):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != 3 * self.n[i]:
+                raise ValueError("state arrays must be contiguous float64 of shape (n, 3)")
         _check(self._lib.pd_sim_get_state(self._h, i, _ptr(x, C.c_double), _ptr(v, C.c_double)))
         return x, v
 
