@@ -322,8 +322,14 @@ class Simulator:
     def set_stream(self, stream_ptr: int | None):
         _check(self._lib.pd_sim_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
+    def _index(self, i: int) -> int:
+        if not 0 <= i < self.count:
+            raise PdError(1, f"instance index {i} out of range (batch of {self.count})")
+        return i
+
     def state(self, i: int = 0, out_x=None, out_v=None):
         """Positions and velocities of instance i (waits for queued work); optional out arrays."""
+        self._index(i)
         x = np.zeros((self.n[i], 3)) if out_x is None else out_x
         v = np.zeros((self.n[i], 3)) if out_v is None else out_v
         for a in (x, v):
