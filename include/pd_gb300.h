@@ -205,6 +205,28 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
 /* Edge colouring (color_of[n_edges]) of the scene; returns the colour count in *colors. */
 int pd_scene_coloring(const pd_mesh* mesh, uint32_t* color_of, int32_t* colors);
 
+/* ---- Allocation-free solve (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc where they solve: a host engine that only hands out
+ * device memory from its own pool, a real-time loop where allocation is banned, a plugin host
+ * that owns the device heap. It solves L x = b for the three x/y/z columns and allocates
+ * nothing: every argument is a DEVICE pointer owned by the caller — the factor exactly as
+ * pd_sim_get_factor / pd_scene_factor export it (perm[n], colptr[n+1], rowidx[nnz], val[nnz],
+ * dinv[n]) and b, x of 3n doubles ([x,y,z] per vertex) — and the only workspace is a fixed
+ * device array built into the library (3 doubles per vertex, PD_NOALLOC_MAX_VERTICES vertices,
+ * 1.5 MiB) that every GPU which loads the library holds until the process exits.
+ * - n > PD_NOALLOC_MAX_VERTICES is rejected with PD_ERR_INVALID_ARGUMENT.
+ * - The first call on a device looks up the workspace's device address for that device; make
+ *   that first call before any stream capture on the device.
+ * - Every call shares the one workspace: calls whose work overlaps on the GPU (different
+ *   streams, or different host threads on one device) race; serialise them on one stream.
+ *   The workspace needs no clearing: each call overwrites all of it that it reads.
+ * - The arithmetic follows the reference's solve order, so x is bit-identical to pd_sim_solve.
+ * The work is queued on `stream` (a cudaStream_t; NULL = default stream) and the call returns
+ * without waiting. */
+#define PD_NOALLOC_MAX_VERTICES 65536
+int pd_solve_noalloc(int32_t n, const int32_t* perm, const int32_t* colptr, const int32_t* rowidx,
+                     const double* val, const double* dinv, const double* b, double* x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,13 @@ int fail(int code, const std::string& msg) {
   g_lastError = msg;
   return code;
 }
+}  // namespace
+
+namespace pdg {
+void setLastError(const std::string& msg) { g_lastError = msg; }
+}  // namespace pdg
+
+namespace {
 int cudaFail(cudaError_t e, const char* what) {
   return fail(PD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
