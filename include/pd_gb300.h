@@ -43,6 +43,7 @@ extern "C" {
 
 /* Arithmetic of the GPU substep. */
 #define PD_PRECISION_FP64_EXACT 0 /* FP64, reference operation order, bit-identical to the CPU path */
+#define PD_PRECISION_FP64 1       /* FP64, supernodal solve (reordered sums, FMA); matches to rounding */
 
 /* Mirror of SceneConfig (core/sim/Scene.h:14-137) plus the fields the synthetic scenes need. */
 typedef struct pd_scene_config {

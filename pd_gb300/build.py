@@ -22,6 +22,7 @@ UNITS = {
     "host.cpp": ["-x", "cu"],
     "abi.cu": [],
     "substep_exact.cu": ["-fmad=false"],
+    "substep_fast.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
 }
 

@@ -84,13 +84,14 @@ struct Instance {
   pdg::Topology topo;
   pdg::ScalarMatrix L;
   pdg::Factor F;
+  pdg::SupernodeTree tree;
   pdg::Stamp stamp;
   std::vector<double> bendRhs;
   int factorizeCount = 0, analyzeCount = 0;
   // arena offsets
   size_t oX, oV, oXn, oXhat, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
-      oEarly, oIters, oConv;
+      oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT;
   size_t bytes = 0;
 };
 
@@ -98,18 +99,20 @@ std::string prepare(Instance& I, bool reanalyze) {
   const auto& c = I.cfg;
   if (!(c.dt > 0.0)) return "dt must be positive";
   if (c.max_iterations < 0) return "max_iterations must be >= 0";
-  if (c.precision != PD_PRECISION_FP64_EXACT) return "unsupported precision mode";
+  if (c.precision != PD_PRECISION_FP64_EXACT && c.precision != PD_PRECISION_FP64)
+    return "unsupported precision mode";
   std::string err = pdg::validateScene(I.scene);
   if (!err.empty()) return err;
   pdg::assembleMatrix(I.scene, c.dt, I.L);
   std::vector<int32_t> perm;
   if (reanalyze || I.F.perm.empty()) {
-    perm = pdg::nestedDissection(I.scene, I.L);
+    perm = pdg::nestedDissection(I.scene, I.L, 24, &I.tree);
     I.analyzeCount += 1;
   } else {
     perm = I.F.perm;
   }
   if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
+  pdg::buildSupernodal(I.F, I.tree);
   I.factorizeCount += 1;
   pdg::assembleBendingRhs(I.scene, I.bendRhs);
   I.stamp = pdg::computeStamp(I.scene, c.dt);
@@ -174,6 +177,16 @@ void layout(Instance& I, Arena& A) {
   I.oEarly = A.zeros(4);
   I.oIters = A.zeros(4);
   I.oConv = A.zeros(4);
+  I.oLvlPtr = A.add(I.F.lvlRowPtr);
+  I.oLvlRows = A.add(I.F.lvlRows);
+  I.oRowSn = A.add(I.F.rowSn);
+  I.oSnStart = A.add(I.F.snStart);
+  I.oOffEnd = A.add(I.F.offEnd);
+  I.oOffBeg = A.add(I.F.offBeg);
+  I.oSnInv = A.add(I.F.snInvOff);
+  I.oInvL = A.add(I.F.invL);
+  I.oInvLT = A.add(I.F.invLT);
+  I.oT = A.zeros(24 * n);
   I.bytes = A.host.size() - before;
 }
 
@@ -235,6 +248,17 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.bwdPtr = reinterpret_cast<const int32_t*>(P(I.oBp));
   d.bwdRows = reinterpret_cast<const int32_t*>(P(I.oBr));
   d.w = reinterpret_cast<double*>(P(I.oW));
+  d.nlevS = static_cast<int32_t>(I.F.lvlRowPtr.size()) - 1;
+  d.lvlRowPtr = reinterpret_cast<const int32_t*>(P(I.oLvlPtr));
+  d.lvlRows = reinterpret_cast<const int32_t*>(P(I.oLvlRows));
+  d.rowSn = reinterpret_cast<const int32_t*>(P(I.oRowSn));
+  d.snStart = reinterpret_cast<const int32_t*>(P(I.oSnStart));
+  d.offEnd = reinterpret_cast<const int32_t*>(P(I.oOffEnd));
+  d.offBeg = reinterpret_cast<const int32_t*>(P(I.oOffBeg));
+  d.snInvOff = reinterpret_cast<const int64_t*>(P(I.oSnInv));
+  d.invL = reinterpret_cast<const double*>(P(I.oInvL));
+  d.invLT = reinterpret_cast<const double*>(P(I.oInvLT));
+  d.tbuf = reinterpret_cast<double*>(P(I.oT));
   d.iterLog = iterLog;
   d.convLog = convLog;
   d.lastResidual = reinterpret_cast<double*>(P(I.oLastRes));
@@ -269,6 +293,7 @@ struct pd_sim {
   int smemBytes = 0;
 
   ~pd_sim() { release(); }
+  int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
   void release() {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
@@ -311,7 +336,8 @@ struct pd_sim {
     int smem = 0;
     for (size_t i = 0; i < inst.size(); ++i) {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
-      const int need = 24 * inst[i].scene.n;
+      // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
+      const int need = (precision() == PD_PRECISION_FP64 ? 48 : 24) * inst[i].scene.n;
       if (need <= kMaxSmem && need > smem) smem = need;
     }
     smemBytes = smem;
@@ -540,6 +566,8 @@ int pd_sim_create_batch(int32_t count, const pd_mesh* meshes, const pd_scene_con
   for (int i = 0; i < count; ++i) {
     Instance& I = sim->inst[i];
     I.cfg = cfgs[i];
+    if (cfgs[i].precision != cfgs[0].precision)
+      return fail(PD_ERR_INVALID_ARGUMENT, "all instances of a batch must use one precision mode");
     int rc = sceneFromMesh(meshes[i], I.scene);
     if (rc != PD_OK) return rc;
     std::string err = pdg::validateScene(I.scene);
@@ -583,7 +611,10 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
     const int rc = s->ensureLogs(substeps);
     if (rc != PD_OK) return rc;
   }
-  const int rc = pdg::launchSubstepExact(s->dDesc, static_cast<int>(s->inst.size()), substeps, s->smemBytes, s->stream);
+  const int count = static_cast<int>(s->inst.size());
+  const int rc = s->precision() == PD_PRECISION_FP64
+                     ? pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream)
+                     : pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
   if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
   s->lastSubsteps = substeps;
   return PD_OK;
@@ -691,7 +722,8 @@ int pd_sim_set_pinned(pd_sim* s, int32_t i, const uint8_t* pinned, const double*
 int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
   if (!s || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
   if (!(cfg->dt > 0.0) || cfg->max_iterations < 0) return fail(PD_ERR_INVALID_ARGUMENT, "invalid dt or iteration count");
-  if (cfg->precision != PD_PRECISION_FP64_EXACT) return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
+  if (cfg->precision != PD_PRECISION_FP64_EXACT && cfg->precision != PD_PRECISION_FP64)
+    return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
   bool refactor = false;
   for (auto& I : s->inst) {
     refactor = refactor || (std::memcmp(&I.cfg.dt, &cfg->dt, sizeof(double)) != 0);
@@ -780,8 +812,11 @@ int pd_sim_solve(pd_sim* s, int32_t i, const double* b, double* x) {
   PD_CUDA(cudaMalloc(&dB, 2 * bytes));
   double* dX = dB + 3 * static_cast<size_t>(I.scene.n);
   PD_CUDA(cudaMemcpyAsync(dB, b, bytes, cudaMemcpyHostToDevice, s->stream));
-  const int smem = (24 * I.scene.n <= kMaxSmem) ? 24 * I.scene.n : 0;
-  const int lrc = pdg::launchSolveExact(s->dDesc + i, dB, dX, smem, s->stream);
+  const bool fast = s->precision() == PD_PRECISION_FP64;
+  const int need = (fast ? 48 : 24) * I.scene.n;
+  const int smem = (need <= kMaxSmem) ? need : 0;
+  const int lrc = fast ? pdg::launchSolveFast(s->dDesc + i, dB, dX, smem, s->stream)
+                       : pdg::launchSolveExact(s->dDesc + i, dB, dX, smem, s->stream);
   if (lrc != 0) {
     cudaFree(dB);
     return cudaFail(static_cast<cudaError_t>(lrc), "solve launch");

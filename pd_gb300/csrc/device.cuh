@@ -61,6 +61,18 @@ struct InstanceDev {
   const int32_t* bwdPtr;
   const int32_t* bwdRows;
   double* w;             // 3n solve workspace in elimination order (global fallback)
+  // supernodal form (nested-dissection tree levels)
+  int32_t nlevS;
+  const int32_t* lvlRowPtr;
+  const int32_t* lvlRows;
+  const int32_t* rowSn;
+  const int32_t* snStart;
+  const int32_t* offEnd;
+  const int32_t* offBeg;
+  const int64_t* snInvOff;
+  const double* invL;
+  const double* invLT;
+  double* tbuf;          // second 3n workspace (global fallback)
   // statistics
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;
@@ -76,6 +88,9 @@ int launchSubstepExact(const InstanceDev* dInstances, int count, int substeps, i
 // Reference-order FP64 3-column solve for one instance: b (3n, vertex order) → x.
 int launchSolveExact(const InstanceDev* dInstance, const double* b, double* x, int smemBytes,
                      void* stream);
+// FP64 substep with the supernodal solve (smem: 6n doubles when they fit).
+int launchSubstepFast(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
+int launchSolveFast(const InstanceDev* dInstance, const double* b, double* x, int smemBytes, void* stream);
 
 constexpr int kBlockThreads = 256;
 

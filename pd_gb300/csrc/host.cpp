@@ -248,17 +248,27 @@ void assembleBendingRhs(const Scene& s, std::vector<double>& out) {
 }
 
 // ------------------------------------------------------------------------------ ordering
-std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int leafSize) {
+std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int leafSize, SupernodeTree* tree) {
   const int n = s.n;
   std::vector<int32_t> order;
   order.reserve(n);
   std::vector<int64_t> mark(n, -1);
   int64_t stamp = 0;
-  std::function<void(std::vector<int32_t>&)> nd = [&](std::vector<int32_t>& verts) {
+  // Each call appends its vertices to `order` and returns the id of the supernode that owns its
+  // last columns (its separator, or itself for a leaf); children get that id as parent.
+  std::vector<int32_t> snBegin, snEnd, snParent;
+  auto newNode = [&](int32_t b, int32_t e) {
+    snBegin.push_back(b);
+    snEnd.push_back(e);
+    snParent.push_back(-1);
+    return static_cast<int32_t>(snBegin.size()) - 1;
+  };
+  std::function<int32_t(std::vector<int32_t>&)> nd = [&](std::vector<int32_t>& verts) -> int32_t {
     if (static_cast<int>(verts.size()) <= leafSize) {
       std::sort(verts.begin(), verts.end());
+      const int32_t b = static_cast<int32_t>(order.size());
       order.insert(order.end(), verts.begin(), verts.end());
-      return;
+      return newNode(b, static_cast<int32_t>(order.size()));
     }
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int v : verts)
@@ -285,18 +295,98 @@ std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int
     }
     if (right.empty() || left.empty()) {  // no progress: treat as a leaf
       std::sort(verts.begin(), verts.end());
+      const int32_t b = static_cast<int32_t>(order.size());
       order.insert(order.end(), verts.begin(), verts.end());
-      return;
+      return newNode(b, static_cast<int32_t>(order.size()));
     }
-    nd(left);
-    nd(right);
+    const int32_t cl = nd(left);
+    const int32_t cr = nd(right);
     std::sort(sep.begin(), sep.end());
+    const int32_t b = static_cast<int32_t>(order.size());
     order.insert(order.end(), sep.begin(), sep.end());
+    const int32_t me = newNode(b, static_cast<int32_t>(order.size()));
+    snParent[cl] = me;
+    snParent[cr] = me;
+    return me;
   };
   std::vector<int32_t> all(n);
   std::iota(all.begin(), all.end(), 0);
   nd(all);
+  if (tree) {
+    // nodes were created in postorder, so their ranges are already ascending and contiguous
+    tree->start.assign(snBegin.size() + 1, 0);
+    for (size_t i = 0; i < snBegin.size(); ++i) tree->start[i] = snBegin[i];
+    tree->start[snBegin.size()] = n;
+    tree->parent = snParent;
+  }
   return order;
+}
+
+// Supernodal data of the factor: splits between off-block and in-block entries, the dense
+// inverse of every diagonal block, and rows grouped by tree level.
+void buildSupernodal(Factor& f, const SupernodeTree& tree) {
+  const int n = f.n;
+  const int ns = static_cast<int>(tree.parent.size());
+  f.snStart = tree.start;
+  f.snParent = tree.parent;
+  f.rowSn.assign(n, 0);
+  for (int s = 0; s < ns; ++s)
+    for (int i = f.snStart[s]; i < f.snStart[s + 1]; ++i) f.rowSn[i] = s;
+  f.offEnd.assign(n, 0);
+  f.offBeg.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    const int s0 = f.snStart[f.rowSn[i]], s1 = f.snStart[f.rowSn[i] + 1];
+    int p = f.rowptr[i];
+    while (p < f.rowptr[i + 1] && f.colidx[p] < s0) ++p;
+    f.offEnd[i] = p;
+    p = f.colptr[i];
+    while (p < f.colptr[i + 1] && f.rowidx[p] < s1) ++p;
+    f.offBeg[i] = p;
+  }
+  // dense inverses of the unit-lower diagonal blocks
+  f.snInvOff.assign(ns + 1, 0);
+  for (int s = 0; s < ns; ++s) {
+    const int64_t sz = f.snStart[s + 1] - f.snStart[s];
+    f.snInvOff[s + 1] = f.snInvOff[s] + sz * (sz + 1) / 2;
+  }
+  f.invL.assign(f.snInvOff[ns], 0.0);
+  f.invLT.assign(f.snInvOff[ns], 0.0);
+  std::vector<double> B, X;
+  for (int s = 0; s < ns; ++s) {
+    const int s0 = f.snStart[s], sz = f.snStart[s + 1] - s0;
+    if (sz == 0) continue;
+    B.assign(static_cast<size_t>(sz) * sz, 0.0);
+    for (int r = 0; r < sz; ++r)
+      for (int p = f.offEnd[s0 + r]; p < f.rowptr[s0 + r + 1]; ++p) B[static_cast<size_t>(r) * sz + (f.colidx[p] - s0)] = f.rowval[p];
+    X.assign(static_cast<size_t>(sz) * sz, 0.0);
+    for (int c = 0; c < sz; ++c) {  // column c of L_SS⁻¹ by forward substitution
+      X[static_cast<size_t>(c) * sz + c] = 1.0;
+      for (int r = c + 1; r < sz; ++r) {
+        double acc = 0.0;
+        for (int t = c; t < r; ++t) acc += B[static_cast<size_t>(r) * sz + t] * X[static_cast<size_t>(t) * sz + c];
+        X[static_cast<size_t>(r) * sz + c] = -acc;
+      }
+    }
+    double* lo = f.invL.data() + f.snInvOff[s];
+    double* up = f.invLT.data() + f.snInvOff[s];
+    for (int r = 0, k = 0; r < sz; ++r)
+      for (int c = 0; c <= r; ++c) lo[k++] = X[static_cast<size_t>(r) * sz + c];
+    for (int r = 0, k = 0; r < sz; ++r)  // row r of the transpose: X[c][r] for c = r..sz−1
+      for (int c = r; c < sz; ++c) up[k++] = X[static_cast<size_t>(c) * sz + r];
+  }
+  // levels: leaves 0, a parent one above its highest child; rows grouped by level
+  f.snLevel.assign(ns, 0);
+  for (int s = 0; s < ns; ++s)  // postorder: children precede parents
+    if (f.snParent[s] >= 0) f.snLevel[f.snParent[s]] = std::max(f.snLevel[f.snParent[s]], f.snLevel[s] + 1);
+  int nlev = 0;
+  for (int s = 0; s < ns; ++s) nlev = std::max(nlev, f.snLevel[s] + 1);
+  f.lvlRowPtr.assign(nlev + 1, 0);
+  for (int s = 0; s < ns; ++s) f.lvlRowPtr[f.snLevel[s] + 1] += f.snStart[s + 1] - f.snStart[s];
+  for (int l = 0; l < nlev; ++l) f.lvlRowPtr[l + 1] += f.lvlRowPtr[l];
+  f.lvlRows.assign(n, 0);
+  std::vector<int32_t> cur(f.lvlRowPtr.begin(), f.lvlRowPtr.end() - 1);
+  for (int s = 0; s < ns; ++s)
+    for (int i = f.snStart[s]; i < f.snStart[s + 1]; ++i) f.lvlRows[cur[f.snLevel[s]]++] = i;
 }
 
 // ----------------------------------------------------------------------- factorization

@@ -62,6 +62,21 @@ struct Factor {
   std::vector<int32_t> parent;          // elimination tree
   // level schedules: rows grouped by dependency depth (forward: leaves first; backward: root first)
   std::vector<int32_t> fwdLevelPtr, fwdRows, bwdLevelPtr, bwdRows;
+
+  // Supernodal form (nested-dissection tree nodes = contiguous column ranges). For a row i of
+  // supernode S = [s0, s1): CSR entries [rowptr[i], offEnd[i]) are the off-block columns (< s0,
+  // all in descendant supernodes); CSC entries [offBeg[k], colptr[k+1]) of a column k in S are the
+  // rows ≥ s1 (all in ancestors). The unit-lower diagonal block of S is kept as its dense inverse.
+  std::vector<int32_t> snStart, snParent, snLevel, rowSn, offEnd, offBeg;
+  std::vector<int64_t> snInvOff;          // offset of S's packed inverse (s(s+1)/2 entries)
+  std::vector<double> invL, invLT;        // packed rows of L_SS⁻¹ and of (L_SS⁻¹)ᵀ
+  std::vector<int32_t> lvlRowPtr, lvlRows; // rows grouped by supernode level (leaves = level 0)
+};
+
+// Nested-dissection tree produced with an ordering: supernode ranges in elimination order.
+struct SupernodeTree {
+  std::vector<int32_t> start;   // ranges [start[s], start[s+1])
+  std::vector<int32_t> parent;  // −1 for roots
 };
 
 void buildTopology(const Scene& s, Topology& t);
@@ -69,7 +84,10 @@ void assembleMatrix(const Scene& s, double dt, ScalarMatrix& L);
 void assembleBendingRhs(const Scene& s, std::vector<double>& out);
 // Nested dissection by recursive coordinate bisection of the rest positions (vertex separators
 // taken from the graph of Ã), leaves in index order.
-std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int leafSize = 24);
+std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int leafSize = 24,
+                                      SupernodeTree* tree = nullptr);
+// Fills the supernodal fields of a factorized Factor from the tree of its ordering.
+void buildSupernodal(Factor& f, const SupernodeTree& tree);
 // Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
 bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
 void buildSchedules(Factor& f);
