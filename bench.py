@@ -29,6 +29,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "PD substeps/s (1 cloth & 512-batch) vs plain FP64 GPU at 1e-5 pos err; grads/s"
+# precision modes of the GPU substep: name -> (PD_PRECISION_* value, dtype label, kernel name)
+PRECISIONS = {"fp64-exact": (0, "f64", "substepExactKernel"), "fp64": (1, "f64", "substepFastKernel")}
 UNIT = "substeps/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -40,6 +42,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--workload", default="cloth40_full")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
     p.add_argument("--batch-count", type=int, default=512)
     p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -53,23 +56,28 @@ def dist_env():
     return rank, world, local
 
 
-def workload(name, batch_count):
+def workload(name, batch_count, precision="fp64"):
+    import copy
     from pd_gb300 import workloads as W
     if name == "batch":
         scenes, cfgs, sub = W.batch(count=batch_count)
-        return scenes, cfgs, sub
-    scenes, cfg, sub = W.WORKLOADS[name]()
-    return scenes, [cfg] * len(scenes), sub
+    else:
+        scenes, cfg, sub = W.WORKLOADS[name]()
+        cfgs = [cfg] * len(scenes)
+    cfgs = [copy.copy(c) for c in cfgs]
+    for c in cfgs:
+        c.precision = PRECISIONS[precision][0]
+    return scenes, cfgs, sub
 
 
-def describe_workload(name, scenes, cfgs):
+def describe_workload(name, scenes, cfgs, precision="fp64"):
     c = cfgs[0]
     n = sum(s.n for s in scenes)
     e = sum(int(s.edges.shape[0]) for s in scenes)
     b = sum(int(np.asarray(s.bends).reshape(-1, 3).shape[0]) for s in scenes)
     return {"workload": name, "instances": len(scenes), "vertices": n, "constraints": e, "bend_stencils": b,
             "iterations": c.max_iterations, "residual_tolerance": c.residual_tolerance, "dt": c.dt,
-            "precision": "fp64-reference-order"}
+            "precision": precision}
 
 
 # --------------------------------------------------------------------------------- roofline
@@ -213,7 +221,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     import pd_gb300 as P
 
-    scenes, cfgs, sub = workload(args.workload, args.batch_count)
+    scenes, cfgs, sub = workload(args.workload, args.batch_count, args.precision)
     sim = P.Simulator(scenes, cfgs)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
@@ -293,8 +301,8 @@ def run_ours(args):
         fp64_achieved = ops / (kernel_ms * 1e-3) / 1e9
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(describe_workload(args.workload, scenes, cfgs),
+                "vs_baseline": None, "dtype": PRECISIONS[args.precision][1], "data": "synthetic",
+                "config": dict(describe_workload(args.workload, scenes, cfgs, args.precision),
                                l2="flushed between timed substeps (256 MB device write outside the timed events)",
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                                factor_nnz=info["factor_nnz"], iterations_used=iters_used[0]),
@@ -302,7 +310,7 @@ def run_ours(args):
                 "gpu_launches": args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                             "kernel": "substepExactKernel",
+                             "kernel": PRECISIONS[args.precision][2],
                              "algorithmic_bytes_per_launch": per_launch_bytes},
                 "fp64": {"achieved_gops": fp64_achieved, "peak_gops": fp64_peak,
                          "frac": fp64_achieved / fp64_peak, "ops_per_launch": ops},

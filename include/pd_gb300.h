@@ -68,6 +68,9 @@ typedef struct pd_scene_config {
   int32_t pin_mode;          /* 0: corners of row ny-1 (reference default); 1: corners of row 0;
                                 2: whole row ny-1; 3: corner (0, ny-1); 4: none */
   int32_t precision;         /* PD_PRECISION_* */
+  int32_t cluster_ctas;      /* PD_PRECISION_FP64: CTAs sharing one cloth (1..16, a thread-block
+                                cluster); 0 = automatic (16 for up to 9 cloths, fewer for larger
+                                batches, 1 = one CTA per cloth) */
 } pd_scene_config;
 
 /* Borrowed host arrays describing one cloth; vectors are [x,y,z] interleaved per vertex.

@@ -37,6 +37,7 @@ class _Cfg(C.Structure):
         ("grid_spacing", C.c_double), ("shear_stiffness", C.c_double), ("bend_stiffness", C.c_double),
         ("bend_sampling", C.c_int32), ("bend_stride", C.c_int32), ("mass_mode", C.c_int32),
         ("total_mass", C.c_double), ("pin_mode", C.c_int32), ("precision", C.c_int32),
+        ("cluster_ctas", C.c_int32),
     ]
 
 
@@ -203,6 +204,7 @@ class SceneConfig:
     total_mass: float = 1.0
     pin_mode: int = 0
     precision: int = PD_PRECISION_FP64_EXACT
+    cluster_ctas: int = 0
 
     def c(self) -> _Cfg:
         c = _Cfg()

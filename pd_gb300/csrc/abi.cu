@@ -91,7 +91,8 @@ struct Instance {
   // arena offsets
   size_t oX, oV, oXn, oXhat, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
-      oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT;
+      oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
+      oLvlG;
   size_t bytes = 0;
 };
 
@@ -119,9 +120,10 @@ std::string prepare(Instance& I, bool reanalyze) {
   return {};
 }
 
-void layout(Instance& I, Arena& A) {
+void layout(Instance& I, Arena& A, int teamCtas) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
+  I.oLvlG = A.add(pdg::chooseGroupWidths(I.F, teamCtas));
   const size_t before = A.host.size();
   I.oX = A.add(s.x);
   I.oV = A.add(s.v);
@@ -259,6 +261,7 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.invL = reinterpret_cast<const double*>(P(I.oInvL));
   d.invLT = reinterpret_cast<const double*>(P(I.oInvLT));
   d.tbuf = reinterpret_cast<double*>(P(I.oT));
+  d.lvlG = reinterpret_cast<const int32_t*>(P(I.oLvlG));
   d.iterLog = iterLog;
   d.convLog = convLog;
   d.lastResidual = reinterpret_cast<double*>(P(I.oLastRes));
@@ -291,9 +294,25 @@ struct pd_sim {
   int logCapacity = 0;
   int lastSubsteps = 0;
   int smemBytes = 0;
+  int teamCtas = 1;  // CTAs per instance (a thread-block cluster when > 1)
 
   ~pd_sim() { release(); }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
+
+  // CTAs per cloth for the supernodal FP64 kernel: the requested count, or 16 for up to nine
+  // cloths (152 SMs / 16) and fewer for larger batches; reduced until the device accepts it.
+  int chooseTeam() const {
+    if (precision() != PD_PRECISION_FP64) return 1;
+    int want = inst[0].cfg.cluster_ctas;
+    if (want <= 0) {
+      const int count = static_cast<int>(inst.size());
+      want = count <= 9 ? 16 : count <= 19 ? 8 : count <= 38 ? 4 : count <= 76 ? 2 : 1;
+    }
+    int cs = 1;
+    while (cs * 2 <= std::min(want, 16)) cs *= 2;
+    while (cs > 1 && pdg::clusterSizeSupported(cs) != cs) cs /= 2;
+    return cs;
+  }
   void release() {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
@@ -308,7 +327,8 @@ struct pd_sim {
 
   int upload(int capacity) {
     Arena A;
-    for (auto& I : inst) layout(I, A);
+    teamCtas = chooseTeam();
+    for (auto& I : inst) layout(I, A, teamCtas);
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -612,9 +632,10 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
     if (rc != PD_OK) return rc;
   }
   const int count = static_cast<int>(s->inst.size());
-  const int rc = s->precision() == PD_PRECISION_FP64
-                     ? pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream)
-                     : pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  int rc;
+  if (s->precision() != PD_PRECISION_FP64) rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  else if (s->teamCtas > 1) rc = pdg::launchSubstepCluster(s->dDesc, count, s->teamCtas, substeps, s->stream);
+  else rc = pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream);
   if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
   s->lastSubsteps = substeps;
   return PD_OK;
@@ -848,7 +869,7 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
   if (dinv) std::memcpy(dinv, F.dinv.data(), F.dinv.size() * 8);
   if (info) {
     Arena A;
-    layout(I, A);
+    layout(I, A, 1);
     info->n_vertices = I.scene.n;
     info->n_edges = static_cast<int32_t>(I.scene.edges.size());
     info->n_bends = static_cast<int32_t>(I.scene.bends.size());

@@ -73,6 +73,7 @@ struct InstanceDev {
   const double* invL;
   const double* invLT;
   double* tbuf;          // second 3n workspace (global fallback)
+  const int32_t* lvlG;   // lanes per row for [level][fwd gather, fwd dense, bwd gather, bwd dense]
   // statistics
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;
@@ -91,6 +92,10 @@ int launchSolveExact(const InstanceDev* dInstance, const double* b, double* x, i
 // FP64 substep with the supernodal solve (smem: 6n doubles when they fit).
 int launchSubstepFast(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
 int launchSolveFast(const InstanceDev* dInstance, const double* b, double* x, int smemBytes, void* stream);
+// FP64 supernodal substep with `clusterSize` CTAs (a thread-block cluster) per instance.
+int launchSubstepCluster(const InstanceDev* dInstances, int count, int clusterSize, int substeps, void* stream);
+// `want` if a cluster of that many 256-thread CTAs can run on this device, else 0.
+int clusterSizeSupported(int want);
 
 constexpr int kBlockThreads = 256;
 

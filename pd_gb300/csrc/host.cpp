@@ -389,6 +389,49 @@ void buildSupernodal(Factor& f, const SupernodeTree& tree) {
     for (int i = f.snStart[s]; i < f.snStart[s + 1]; ++i) f.lvlRows[cur[f.snLevel[s]]++] = i;
 }
 
+std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
+  const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
+  std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
+  const double smsps = 4.0 * teamCtas, threads = 256.0 * teamCtas;
+  for (int l = 0; l < nlev; ++l) {
+    for (int ph = 0; ph < 4; ++ph) {
+      const int R = f.lvlRowPtr[l + 1] - f.lvlRowPtr[l];
+      if (R == 0) continue;
+      double sum = 0.0;
+      int lmax = 0;
+      for (int t = f.lvlRowPtr[l]; t < f.lvlRowPtr[l + 1]; ++t) {
+        const int i = f.lvlRows[t];
+        const int s = f.rowSn[i], s0 = f.snStart[s], sz = f.snStart[s + 1] - s0;
+        int len = 0;
+        switch (ph) {
+          case 0: len = f.offEnd[i] - f.rowptr[i]; break;
+          case 1: len = i - s0 + 1; break;
+          case 2: len = f.colptr[i + 1] - f.offBeg[i]; break;
+          default: len = sz - (i - s0); break;
+        }
+        sum += len;
+        lmax = std::max(lmax, len);
+      }
+      const double lavg = sum / R;
+      double best = 1e300;
+      int bestG = 1;
+      for (int G = 1, lg = 0; G <= 32; G *= 2, ++lg) {
+        const double perRowInstr = 3.0 * std::ceil(lavg / G) + 3.0 * lg + 3.0;
+        const double total = R * G / 32.0 * perRowInstr;                 // warp instructions
+        const double rowsPerGroup = std::ceil(R * G / threads);
+        const double chain = rowsPerGroup * (3.0 * std::ceil(static_cast<double>(lmax) / G) + 3.0 * lg + 3.0);
+        const double cost = std::max(total / smsps, chain);
+        if (cost < best) {
+          best = cost;
+          bestG = G;
+        }
+      }
+      g[4 * static_cast<size_t>(l) + ph] = bestG;
+    }
+  }
+  return g;
+}
+
 // ----------------------------------------------------------------------- factorization
 // Up-looking LDLᵀ: the published algorithm of T. A. Davis' LDL package, which Eigen 3.4.0's
 // SimplicialLDLT implements. Row k of L comes from a sparse triangular solve whose pattern is

@@ -88,6 +88,11 @@ std::vector<int32_t> nestedDissection(const Scene& s, const ScalarMatrix& L, int
                                       SupernodeTree* tree = nullptr);
 // Fills the supernodal fields of a factorized Factor from the tree of its ordering.
 void buildSupernodal(Factor& f, const SupernodeTree& tree);
+// Lanes per row (1..32) for each level and phase of the supernodal solve run by `teamCtas` CTAs
+// of 256 threads, from a cost model of FP64 warp instructions: on GB300 an FP64 warp
+// instruction occupies its SMSP's pipe for ~80 cycles whatever its active lanes, so narrow groups
+// waste fewer lanes while wide groups spread a level's few long rows over more SMSPs.
+std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas);
 // Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
 bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
 void buildSchedules(Factor& f);

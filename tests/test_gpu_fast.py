@@ -17,9 +17,10 @@ pytestmark = pytest.mark.gpu
 TOL_POS = 1e-10
 
 
-def fast(cfg):
+def fast(cfg, ctas=0):
     c = copy.copy(cfg)
     c.precision = 1
+    c.cluster_ctas = ctas
     return c
 
 
@@ -33,10 +34,11 @@ def test_solve_matches_oracle(pdg):
         assert max_rel(sim.solve(b), orc.solve(b)) < 1e-13
 
 
+@pytest.mark.parametrize("ctas", [1, 4, 16])
 @pytest.mark.parametrize("name,substeps", [("cloth40_plain", 600), ("cloth40_full", 120)])
-def test_trajectory_within_tolerance(pdg, name, substeps):
+def test_trajectory_within_tolerance(pdg, name, substeps, ctas):
     scenes, cfg, _ = W.WORKLOADS[name]()
-    sim = pdg.Simulator(scenes[0], fast(cfg))
+    sim = pdg.Simulator(scenes[0], fast(cfg, ctas))
     orc = oracle_twin(scenes[0], cfg, perm=sim.factor()["perm"])
     sim.step(substeps)
     it_g, _ = sim.iteration_log()
@@ -50,9 +52,24 @@ def test_trajectory_within_tolerance(pdg, name, substeps):
     assert np.array_equal(xg[pins], scenes[0].positions[pins])
 
 
-def test_batch_fast_matches_oracle(pdg):
+def test_cluster_without_replicas_matches_oracle(pdg):
+    """A 60×60 cloth needs more than the shared-memory replicas hold: the cluster keeps its
+    workspaces in L2 instead."""
+    cfg = fast(W._base(grid_nx=60, grid_ny=60, grid_spacing=1 / 59, max_iterations=10, shear_stiffness=1000.0,
+                       bend_stiffness=50.0), 16)
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    sim.step(40)
+    it_o, _ = orc.step(40)
+    assert np.array_equal(sim.iteration_log()[0], it_o)
+    assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
+
+
+@pytest.mark.parametrize("ctas", [1, 8])
+def test_batch_fast_matches_oracle(pdg, ctas):
     scenes, cfgs, _ = W.batch(count=6, seed=21, max_side=48)
-    cfgs = [fast(c) for c in cfgs]
+    cfgs = [fast(c, ctas) for c in cfgs]
     sim = pdg.Simulator(scenes, cfgs)
     sim.step(30)
     for i, (s, c) in enumerate(zip(scenes, cfgs)):
@@ -63,9 +80,10 @@ def test_batch_fast_matches_oracle(pdg):
         assert max_rel(xg, xo) < TOL_POS, i
 
 
-def test_gate_decisions_match_in_fast_mode(pdg):
+@pytest.mark.parametrize("ctas", [1, 16])
+def test_gate_decisions_match_in_fast_mode(pdg, ctas):
     cfg = fast(W._base(grid_nx=12, grid_ny=12, grid_spacing=0.05, max_iterations=30, residual_tolerance=0.3,
-                       velocity_damping=0.02))
+                       velocity_damping=0.02), ctas)
     scene = pdg.make_grid(cfg)
     sim = pdg.Simulator(scene, cfg)
     orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
