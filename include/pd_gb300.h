@@ -44,6 +44,9 @@ extern "C" {
 /* Arithmetic of the GPU substep. */
 #define PD_PRECISION_FP64_EXACT 0 /* FP64, reference operation order, bit-identical to the CPU path */
 #define PD_PRECISION_FP64 1       /* FP64, supernodal solve (reordered sums, FMA); matches to rounding */
+#define PD_PRECISION_FP32_PROJECTION 2 /* projection in FP32 accumulated into an FP64 b; FP64 solve */
+#define PD_PRECISION_FP32_SOLVE 3 /* FP32 supernodal solve + one FP64 iterative-refinement step */
+#define PD_PRECISION_MIXED 4      /* FP32 projection and FP32 solve + one FP64 refinement step */
 
 /* Mirror of SceneConfig (core/sim/Scene.h:14-137) plus the fields the synthetic scenes need. */
 typedef struct pd_scene_config {
@@ -71,7 +74,12 @@ typedef struct pd_scene_config {
   int32_t cluster_ctas;      /* PD_PRECISION_FP64: CTAs sharing one cloth (1..16, a thread-block
                                 cluster); 0 = automatic (16 for up to 9 cloths, fewer for larger
                                 batches, 1 = one CTA per cloth) */
+  int32_t dense_max_vertices; /* FP32_SOLVE / MIXED with a cluster: solve with the explicit FP32
+                                 inverse of Ã when every cloth has at most this many vertices
+                                 (0 = PD_DENSE_DEFAULT_MAX_VERTICES, < 0 = never) */
 } pd_scene_config;
+
+#define PD_DENSE_DEFAULT_MAX_VERTICES 3072
 
 /* Borrowed host arrays describing one cloth; vectors are [x,y,z] interleaved per vertex.
  * velocities / pin_positions may be NULL (zero velocity; pins at the current positions, as
@@ -155,7 +163,15 @@ typedef struct pd_sim_info {
   int32_t factorize_count;       /* SimContext::factorizeCount */
   int32_t analyze_count;
   int64_t device_bytes;          /* device memory held by this instance */
+  int32_t cluster_ctas;          /* CTAs running each cloth */
+  int32_t solve_kind;            /* PD_SOLVE_* */
 } pd_sim_info;
+
+/* How the substep kernel solves L·x = b. */
+#define PD_SOLVE_LEVELS 0        /* FP64 level-scheduled rows in the reference's order */
+#define PD_SOLVE_SUPERNODAL 1    /* FP64 nested-dissection supernodes */
+#define PD_SOLVE_SUPERNODAL32 2  /* FP32 supernodes + one FP64 refinement step */
+#define PD_SOLVE_DENSE32 3       /* explicit FP32 inverse + one FP64 refinement step */
 
 typedef struct pd_sim_stats {    /* SimContext counters (core/sim/Scene.h:161-169) */
   int32_t iterations_used;       /* of the last substep */

@@ -6,6 +6,14 @@ bindings raises if the library is missing.
 """
 from .api import (  # noqa: F401
     PD_PRECISION_FP64_EXACT,
+    PD_PRECISION_FP64,
+    PD_PRECISION_FP32_PROJECTION,
+    PD_PRECISION_FP32_SOLVE,
+    PD_PRECISION_MIXED,
+    PD_SOLVE_LEVELS,
+    PD_SOLVE_SUPERNODAL,
+    PD_SOLVE_SUPERNODAL32,
+    PD_SOLVE_DENSE32,
     PdError,
     SceneConfig,
     GridScene,

@@ -16,7 +16,15 @@ from dataclasses import dataclass, field, fields
 import numpy as np
 
 PD_OK = 0
-PD_PRECISION_FP64_EXACT = 0
+PD_PRECISION_FP64_EXACT = 0       # FP64 in the reference's operation order (bit-identical)
+PD_PRECISION_FP64 = 1             # FP64, supernodal solve (matches to rounding)
+PD_PRECISION_FP32_PROJECTION = 2  # FP32 projection, FP64 supernodal solve
+PD_PRECISION_FP32_SOLVE = 3       # FP32 solve + one FP64 refinement step
+PD_PRECISION_MIXED = 4            # FP32 projection + FP32 solve + FP64 refinement
+PD_SOLVE_LEVELS = 0               # solve kinds reported by Simulator.info()["solve_kind"]
+PD_SOLVE_SUPERNODAL = 1
+PD_SOLVE_SUPERNODAL32 = 2
+PD_SOLVE_DENSE32 = 3
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpd_gb300.so")
@@ -37,7 +45,7 @@ class _Cfg(C.Structure):
         ("grid_spacing", C.c_double), ("shear_stiffness", C.c_double), ("bend_stiffness", C.c_double),
         ("bend_sampling", C.c_int32), ("bend_stride", C.c_int32), ("mass_mode", C.c_int32),
         ("total_mass", C.c_double), ("pin_mode", C.c_int32), ("precision", C.c_int32),
-        ("cluster_ctas", C.c_int32),
+        ("cluster_ctas", C.c_int32), ("dense_max_vertices", C.c_int32),
     ]
 
 
@@ -61,6 +69,7 @@ class _SimInfo(C.Structure):
         ("color_count", C.c_int32), ("matrix_nnz", C.c_int64), ("factor_nnz", C.c_int64),
         ("forward_levels", C.c_int32), ("backward_levels", C.c_int32),
         ("factorize_count", C.c_int32), ("analyze_count", C.c_int32), ("device_bytes", C.c_int64),
+        ("cluster_ctas", C.c_int32), ("solve_kind", C.c_int32),
     ]
 
 
@@ -205,6 +214,7 @@ class SceneConfig:
     pin_mode: int = 0
     precision: int = PD_PRECISION_FP64_EXACT
     cluster_ctas: int = 0
+    dense_max_vertices: int = 0
 
     def c(self) -> _Cfg:
         c = _Cfg()

@@ -23,6 +23,7 @@ UNITS = {
     "abi.cu": [],
     "substep_exact.cu": ["-fmad=false"],
     "substep_fast.cu": [],
+    "substep_mixed.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
 }
 

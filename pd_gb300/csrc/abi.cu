@@ -92,16 +92,26 @@ struct Instance {
   size_t oX, oV, oXn, oXhat, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
-      oLvlG;
+      oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
+      oVptr, oVcol, oVval;
+  int denseLd = 0;  // > 0: Ã⁻¹ is in the arena
   size_t bytes = 0;
 };
+
+bool validPrecision(int p) { return p >= PD_PRECISION_FP64_EXACT && p <= PD_PRECISION_MIXED; }
+// FP64 supernodal solve (with FP64 or FP32 projection)
+bool supernodalFp64(int p) { return p == PD_PRECISION_FP64 || p == PD_PRECISION_FP32_PROJECTION; }
+// FP32 solve + FP64 refinement
+bool mixedSolve(int p) { return p == PD_PRECISION_FP32_SOLVE || p == PD_PRECISION_MIXED; }
+bool projection32(int p) { return p == PD_PRECISION_FP32_PROJECTION || p == PD_PRECISION_MIXED; }
+// bytes of per-CTA workspace: reference order w; supernodal w, t; mixed B, X0 (FP64) and Y, T (FP32)
+int workspaceBytesPerVertex(int p) { return mixedSolve(p) ? 72 : (p == PD_PRECISION_FP64_EXACT ? 24 : 48); }
 
 std::string prepare(Instance& I, bool reanalyze) {
   const auto& c = I.cfg;
   if (!(c.dt > 0.0)) return "dt must be positive";
   if (c.max_iterations < 0) return "max_iterations must be >= 0";
-  if (c.precision != PD_PRECISION_FP64_EXACT && c.precision != PD_PRECISION_FP64)
-    return "unsupported precision mode";
+  if (!validPrecision(c.precision)) return "unsupported precision mode";
   std::string err = pdg::validateScene(I.scene);
   if (!err.empty()) return err;
   pdg::assembleMatrix(I.scene, c.dt, I.L);
@@ -114,16 +124,25 @@ std::string prepare(Instance& I, bool reanalyze) {
   }
   if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
   pdg::buildSupernodal(I.F, I.tree);
+  pdg::buildMixed(I.F, I.L);
   I.factorizeCount += 1;
   pdg::assembleBendingRhs(I.scene, I.bendRhs);
   I.stamp = pdg::computeStamp(I.scene, c.dt);
   return {};
 }
 
-void layout(Instance& I, Arena& A, int teamCtas) {
+void layout(Instance& I, Arena& A, int teamCtas, bool dense) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
   I.oLvlG = A.add(pdg::chooseGroupWidths(I.F, teamCtas));
+  I.denseLd = 0;
+  I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
+  if (dense) {
+    I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
+    I.oVptr = A.add(I.L.rowptr);
+    I.oVcol = A.add(I.L.col);
+    I.oVval = A.add(I.L.val);
+  }
   const size_t before = A.host.size();
   I.oX = A.add(s.x);
   I.oV = A.add(s.v);
@@ -189,6 +208,18 @@ void layout(Instance& I, Arena& A, int teamCtas) {
   I.oInvL = A.add(I.F.invL);
   I.oInvLT = A.add(I.F.invLT);
   I.oT = A.zeros(24 * n);
+  I.oLvlG32 = A.add(pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads : pdg::kBlockThreads));
+  I.oLrv32 = A.add(I.F.rowval32);
+  I.oLcv32 = A.add(I.F.colval32);
+  I.oInvL32 = A.add(I.F.invL32);
+  I.oInvLT32 = A.add(I.F.invLT32);
+  I.oDinv32 = A.add(I.F.dinv32);
+  I.oAptr = A.add(I.F.Aptr);
+  I.oAcol = A.add(I.F.Acol);
+  I.oAval = A.add(I.F.Aval);
+  I.oX0 = A.zeros(24 * n);
+  I.oY32 = A.zeros(12 * n);
+  I.oT32 = A.zeros(12 * n);
   I.bytes = A.host.size() - before;
 }
 
@@ -262,6 +293,26 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.invLT = reinterpret_cast<const double*>(P(I.oInvLT));
   d.tbuf = reinterpret_cast<double*>(P(I.oT));
   d.lvlG = reinterpret_cast<const int32_t*>(P(I.oLvlG));
+  d.proj32 = projection32(c.precision) ? 1 : 0;
+  d.lvlG32 = reinterpret_cast<const int32_t*>(P(I.oLvlG32));
+  d.Lrv32 = reinterpret_cast<const float*>(P(I.oLrv32));
+  d.Lcv32 = reinterpret_cast<const float*>(P(I.oLcv32));
+  d.invL32 = reinterpret_cast<const float*>(P(I.oInvL32));
+  d.invLT32 = reinterpret_cast<const float*>(P(I.oInvLT32));
+  d.dinv32 = reinterpret_cast<const float*>(P(I.oDinv32));
+  d.Aptr = reinterpret_cast<const int32_t*>(P(I.oAptr));
+  d.Acol = reinterpret_cast<const int32_t*>(P(I.oAcol));
+  d.Aval = reinterpret_cast<const double*>(P(I.oAval));
+  d.x0 = reinterpret_cast<double*>(P(I.oX0));
+  d.y32 = reinterpret_cast<float*>(P(I.oY32));
+  d.t32 = reinterpret_cast<float*>(P(I.oT32));
+  d.denseLd = I.denseLd;
+  if (I.denseLd > 0) {
+    d.Ainv = reinterpret_cast<const float*>(P(I.oAinv));
+    d.Vptr = reinterpret_cast<const int32_t*>(P(I.oVptr));
+    d.Vcol = reinterpret_cast<const int32_t*>(P(I.oVcol));
+    d.Vval = reinterpret_cast<const double*>(P(I.oVval));
+  }
   d.iterLog = iterLog;
   d.convLog = convLog;
   d.lastResidual = reinterpret_cast<double*>(P(I.oLastRes));
@@ -295,14 +346,24 @@ struct pd_sim {
   int lastSubsteps = 0;
   int smemBytes = 0;
   int teamCtas = 1;  // CTAs per instance (a thread-block cluster when > 1)
+  bool dense = false;  // mixed modes: the cluster applies the explicit FP32 inverse
 
   ~pd_sim() { release(); }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
 
   // CTAs per cloth for the supernodal FP64 kernel: the requested count, or 16 for up to nine
   // cloths (152 SMs / 16) and fewer for larger batches; reduced until the device accepts it.
-  int chooseTeam() const {
-    if (precision() != PD_PRECISION_FP64) return 1;
+  // Mixed modes: every CTA of the cluster solves in its own shared memory, so a cluster needs
+  // 72·n bytes of it per CTA.
+  // Sets teamCtas and dense. CTAs per cloth: the requested count, or 16 for up to nine cloths
+  // (152 SMs / 16) and fewer for larger batches, reduced until the device accepts it. Mixed modes
+  // with a cluster apply the explicit FP32 inverse when every cloth is small enough; otherwise
+  // every CTA of the cluster solves in its own shared memory (72·n bytes per CTA).
+  void planTeam() {
+    const int p = precision();
+    teamCtas = 1;
+    dense = false;
+    if (p == PD_PRECISION_FP64_EXACT) return;
     int want = inst[0].cfg.cluster_ctas;
     if (want <= 0) {
       const int count = static_cast<int>(inst.size());
@@ -310,9 +371,35 @@ struct pd_sim {
     }
     int cs = 1;
     while (cs * 2 <= std::min(want, 16)) cs *= 2;
-    while (cs > 1 && pdg::clusterSizeSupported(cs) != cs) cs /= 2;
-    return cs;
+    if (!mixedSolve(p)) {
+      while (cs > 1 && pdg::clusterSizeSupported(cs) != cs) cs /= 2;
+      teamCtas = cs;
+      return;
+    }
+    int maxN = 0;
+    for (const auto& I : inst) maxN = std::max(maxN, I.scene.n);
+    if (cs > 1 && maxN <= denseLimit()) {
+      int d = cs;
+      while (d > 1 && pdg::denseClusterSupported(d, denseSmem(maxN)) != d) d /= 2;
+      if (d > 1) {
+        teamCtas = d;
+        dense = true;
+        return;
+      }
+    }
+    if (72 * maxN > kMaxSmem) return;
+    while (cs > 1 && pdg::mixedClusterSupported(cs, 72 * maxN) != cs) cs /= 2;
+    teamCtas = cs;
   }
+  // Largest cloth solved with the explicit inverse: the configured limit, capped by the
+  // kernel's shared memory (denseSmem(n) ≤ kMaxSmem).
+  int denseLimit() const {
+    const int v = inst[0].cfg.dense_max_vertices;
+    const int want = v == 0 ? PD_DENSE_DEFAULT_MAX_VERTICES : v;
+    return want > 0 ? std::min(want, kMaxSmem / 60 / 32 * 32) : 0;
+  }
+  // dense-inverse kernel workspace: b and x₀ in FP64, three padded FP32 vectors
+  static int denseSmem(int n) { return 48 * n + 12 * ((n + 31) / 32 * 32); }
   void release() {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
@@ -327,8 +414,8 @@ struct pd_sim {
 
   int upload(int capacity) {
     Arena A;
-    teamCtas = chooseTeam();
-    for (auto& I : inst) layout(I, A, teamCtas);
+    planTeam();
+    for (auto& I : inst) layout(I, A, teamCtas, dense);
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -357,7 +444,7 @@ struct pd_sim {
     for (size_t i = 0; i < inst.size(); ++i) {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
-      const int need = (precision() == PD_PRECISION_FP64 ? 48 : 24) * inst[i].scene.n;
+      const int need = dense ? denseSmem(inst[i].scene.n) : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       if (need <= kMaxSmem && need > smem) smem = need;
     }
     smemBytes = smem;
@@ -633,9 +720,18 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
   }
   const int count = static_cast<int>(s->inst.size());
   int rc;
-  if (s->precision() != PD_PRECISION_FP64) rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
-  else if (s->teamCtas > 1) rc = pdg::launchSubstepCluster(s->dDesc, count, s->teamCtas, substeps, s->stream);
-  else rc = pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  const int p = s->precision();
+  if (p == PD_PRECISION_FP64_EXACT) {
+    rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  } else if (s->dense) {
+    rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
+  } else if (mixedSolve(p)) {
+    rc = s->teamCtas > 1 ? pdg::launchSubstepMixedCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream)
+                         : pdg::launchSubstepMixed(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  } else {
+    rc = s->teamCtas > 1 ? pdg::launchSubstepCluster(s->dDesc, count, s->teamCtas, substeps, s->stream)
+                         : pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  }
   if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
   s->lastSubsteps = substeps;
   return PD_OK;
@@ -743,7 +839,7 @@ int pd_sim_set_pinned(pd_sim* s, int32_t i, const uint8_t* pinned, const double*
 int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
   if (!s || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
   if (!(cfg->dt > 0.0) || cfg->max_iterations < 0) return fail(PD_ERR_INVALID_ARGUMENT, "invalid dt or iteration count");
-  if (cfg->precision != PD_PRECISION_FP64_EXACT && cfg->precision != PD_PRECISION_FP64)
+  if (!validPrecision(cfg->precision))
     return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
   bool refactor = false;
   for (auto& I : s->inst) {
@@ -779,6 +875,12 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   out->factorize_count = I.factorizeCount;
   out->analyze_count = I.analyzeCount;
   out->device_bytes = static_cast<int64_t>(I.bytes);
+  out->cluster_ctas = s->teamCtas;
+  const int p = s->precision();
+  out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
+                    : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
+                    : s->dense                   ? PD_SOLVE_DENSE32
+                                                 : PD_SOLVE_SUPERNODAL32;
   return PD_OK;
 }
 
@@ -833,7 +935,7 @@ int pd_sim_solve(pd_sim* s, int32_t i, const double* b, double* x) {
   PD_CUDA(cudaMalloc(&dB, 2 * bytes));
   double* dX = dB + 3 * static_cast<size_t>(I.scene.n);
   PD_CUDA(cudaMemcpyAsync(dB, b, bytes, cudaMemcpyHostToDevice, s->stream));
-  const bool fast = s->precision() == PD_PRECISION_FP64;
+  const bool fast = s->precision() != PD_PRECISION_FP64_EXACT;
   const int need = (fast ? 48 : 24) * I.scene.n;
   const int smem = (need <= kMaxSmem) ? need : 0;
   const int lrc = fast ? pdg::launchSolveFast(s->dDesc + i, dB, dX, smem, s->stream)
@@ -869,7 +971,11 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
   if (dinv) std::memcpy(dinv, F.dinv.data(), F.dinv.size() * 8);
   if (info) {
     Arena A;
-    layout(I, A, 1);
+    layout(I, A, 1, false);
+    info->cluster_ctas = 1;
+    info->solve_kind = I.cfg.precision == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
+                       : mixedSolve(I.cfg.precision)              ? PD_SOLVE_SUPERNODAL32
+                                                                  : PD_SOLVE_SUPERNODAL;
     info->n_vertices = I.scene.n;
     info->n_edges = static_cast<int32_t>(I.scene.edges.size());
     info->n_bends = static_cast<int32_t>(I.scene.bends.size());

@@ -74,6 +74,27 @@ struct InstanceDev {
   const double* invLT;
   double* tbuf;          // second 3n workspace (global fallback)
   const int32_t* lvlG;   // lanes per row for [level][fwd gather, fwd dense, bwd gather, bwd dense]
+  // mixed precision
+  int32_t proj32;        // projection (d_e) computed in FP32, accumulated in FP64
+  const int32_t* lvlG32; // lanes per row for the one-CTA FP32 solve
+  const float* Lrv32;
+  const float* Lcv32;
+  const float* invL32;
+  const float* invLT32;
+  const float* dinv32;
+  const int32_t* Aptr;   // Ã in elimination order (FP64 refinement residual)
+  const int32_t* Acol;
+  const double* Aval;
+  double* x0;            // 3n global fallback workspaces of the one-CTA mixed kernel
+  float* y32;
+  float* t32;
+  // dense-inverse solve for small cloths: Ã⁻¹ in vertex order (FP32, rows padded to denseLd) and
+  // Ã in vertex order (FP64) for the refinement residual
+  int32_t denseLd;
+  const float* Ainv;
+  const int32_t* Vptr;
+  const int32_t* Vcol;
+  const double* Vval;
   // statistics
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;
@@ -96,7 +117,22 @@ int launchSolveFast(const InstanceDev* dInstance, const double* b, double* x, in
 int launchSubstepCluster(const InstanceDev* dInstances, int count, int clusterSize, int substeps, void* stream);
 // `want` if a cluster of that many 256-thread CTAs can run on this device, else 0.
 int clusterSizeSupported(int want);
+// Mixed-precision substep (FP32 solve + one FP64 refinement step): one CTA per instance with
+// smemBytes of workspace (72·n when it fits, else 0 = global), or a cluster of clusterSize CTAs
+// per instance, each CTA solving the whole system in its own shared memory (72·max n bytes).
+int launchSubstepMixed(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
+int launchSubstepMixedCluster(const InstanceDev* dInstances, int count, int clusterSize, int smemBytes, int substeps,
+                              void* stream);
+int mixedClusterSupported(int clusterSize, int smemBytes);
+// Mixed-precision substep for small cloths with the explicit FP32 inverse: the cluster splits
+// the rows of Ã⁻¹ (smemBytes = 48·n + 12·denseLd).
+int launchSubstepDenseCluster(const InstanceDev* dInstances, int count, int clusterSize, int smemBytes, int substeps,
+                              void* stream);
+int denseClusterSupported(int clusterSize, int smemBytes);
 
-constexpr int kBlockThreads = 256;
+constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
+                                      // the CTAs of the FP64 cluster kernel (fewer threads per
+                                      // barrier beat more threads per level there)
+constexpr int kClusterThreads = 1024; // mixed cluster kernels: one CTA fills its SM to hide L2 latency
 
 }  // namespace pdg

@@ -389,9 +389,110 @@ void buildSupernodal(Factor& f, const SupernodeTree& tree) {
     for (int i = f.snStart[s]; i < f.snStart[s + 1]; ++i) f.lvlRows[cur[f.snLevel[s]]++] = i;
 }
 
+namespace {
+// Row length of row i of the supernodal solve for phase ph (fwd gather, fwd dense, bwd gather, bwd dense).
+int phaseLength(const Factor& f, int i, int ph) {
+  const int s = f.rowSn[i], s0 = f.snStart[s], sz = f.snStart[s + 1] - s0;
+  switch (ph) {
+    case 0: return f.offEnd[i] - f.rowptr[i];
+    case 1: return i - s0 + 1;
+    case 2: return f.colptr[i + 1] - f.offBeg[i];
+    default: return sz - (i - s0);
+  }
+}
+}  // namespace
+
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads) {
+  const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
+  std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
+  for (int l = 0; l < nlev; ++l)
+    for (int ph = 0; ph < 4; ++ph) {
+      const int R = f.lvlRowPtr[l + 1] - f.lvlRowPtr[l];
+      if (R == 0) continue;
+      double sum = 0.0;
+      int lmax = 0;
+      for (int t = f.lvlRowPtr[l]; t < f.lvlRowPtr[l + 1]; ++t) {
+        const int len = phaseLength(f, f.lvlRows[t], ph);
+        sum += len;
+        lmax = std::max(lmax, len);
+      }
+      const double lavg = sum / R;
+      double best = 1e300;
+      int bestG = 1;
+      for (int G = 1, lg = 0; G <= 32; G *= 2, ++lg) {
+        // one CTA of 256 threads: issue-bound term (1 warp instruction per cycle per SMSP) against
+        // the longest group's latency chain: an L2 round trip (~600 cycles) per four unrolled
+        // trips of the row loop, ~8 cycles per dependent FMA, ~30 per shuffle step
+        const double trips = std::ceil(static_cast<double>(lmax) / G);
+        const double issue = R * G / 32.0 * (3.0 * std::ceil(lavg / G) + 4.0 * lg + 6.0) / 4.0;
+        const double chain = std::ceil(R * G / static_cast<double>(ctaThreads)) *
+                             (600.0 * std::ceil(trips / 4.0) + 8.0 * trips + 30.0 * lg + 600.0);
+        const double cost = std::max(issue, chain);
+        if (cost < best) {
+          best = cost;
+          bestG = G;
+        }
+      }
+      g[4 * static_cast<size_t>(l) + ph] = bestG;
+    }
+  return g;
+}
+
+void buildMixed(Factor& f, const ScalarMatrix& A) {
+  auto toF = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+  f.rowval32 = toF(f.rowval);
+  f.colval32 = toF(f.colval);
+  f.invL32 = toF(f.invL);
+  f.invLT32 = toF(f.invLT);
+  f.dinv32 = toF(f.dinv);
+  const int n = f.n;
+  f.Aptr.assign(n + 1, 0);
+  f.Acol.clear();
+  f.Aval.clear();
+  std::vector<std::pair<int32_t, double>> row;
+  for (int i = 0; i < n; ++i) {
+    const int v = f.perm[i];
+    row.clear();
+    for (int p = A.rowptr[v]; p < A.rowptr[v + 1]; ++p) row.push_back({f.iperm[A.col[p]], A.val[p]});
+    std::sort(row.begin(), row.end(), [](auto& a, auto& b) { return a.first < b.first; });
+    for (auto& e : row) {
+      f.Acol.push_back(e.first);
+      f.Aval.push_back(e.second);
+    }
+    f.Aptr[i + 1] = static_cast<int32_t>(f.Acol.size());
+  }
+}
+
+std::vector<float> denseInverse32(const Factor& f, int* ldOut) {
+  const int n = f.n;
+  const int ld = (n + 31) / 32 * 32;
+  *ldOut = ld;
+  std::vector<float> M(static_cast<size_t>(n) * ld, 0.0f);
+  std::vector<double> w(n);
+  for (int v = 0; v < n; ++v) {  // column v of Ã⁻¹ = solve(e_v)
+    std::fill(w.begin(), w.end(), 0.0);
+    w[f.iperm[v]] = 1.0;
+    for (int k = 0; k < n; ++k) {
+      const double yk = w[k];
+      if (yk != 0.0)
+        for (int p = f.colptr[k]; p < f.colptr[k + 1]; ++p) w[f.rowidx[p]] -= f.colval[p] * yk;
+    }
+    for (int k = 0; k < n; ++k) w[k] *= f.dinv[k];
+    for (int k = n - 1; k >= 0; --k) {
+      double acc = w[k];
+      for (int p = f.colptr[k]; p < f.colptr[k + 1]; ++p) acc -= f.colval[p] * w[f.rowidx[p]];
+      w[k] = acc;
+    }
+    float* row = M.data() + static_cast<size_t>(v) * ld;  // symmetric: row v = column v
+    for (int u = 0; u < n; ++u) row[u] = static_cast<float>(w[f.iperm[u]]);
+  }
+  return M;
+}
+
 std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
   const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
   std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
+  // every CTA of the FP64 kernels runs 256 threads
   const double smsps = 4.0 * teamCtas, threads = 256.0 * teamCtas;
   for (int l = 0; l < nlev; ++l) {
     for (int ph = 0; ph < 4; ++ph) {
@@ -416,10 +517,14 @@ std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
       double best = 1e300;
       int bestG = 1;
       for (int G = 1, lg = 0; G <= 32; G *= 2, ++lg) {
+        // cycles: FP64 warp instructions spread over the team's SMSPs (~80 cycles each) against
+        // the longest group's chain — an L2 round trip (~700 cycles) per four unrolled trips,
+        // 64 cycles per dependent FP64 FMA, ~100 per shuffle-and-add step, one more round trip
         const double perRowInstr = 3.0 * std::ceil(lavg / G) + 3.0 * lg + 3.0;
-        const double total = R * G / 32.0 * perRowInstr;                 // warp instructions
+        const double total = R * G / 32.0 * perRowInstr * 80.0;
         const double rowsPerGroup = std::ceil(R * G / threads);
-        const double chain = rowsPerGroup * (3.0 * std::ceil(static_cast<double>(lmax) / G) + 3.0 * lg + 3.0);
+        const double trips = std::ceil(static_cast<double>(lmax) / G);
+        const double chain = rowsPerGroup * (700.0 * std::ceil(trips / 4.0) + 64.0 * trips + 100.0 * lg + 700.0);
         const double cost = std::max(total / smsps, chain);
         if (cost < best) {
           best = cost;

@@ -71,6 +71,12 @@ struct Factor {
   std::vector<int64_t> snInvOff;          // offset of S's packed inverse (s(s+1)/2 entries)
   std::vector<double> invL, invLT;        // packed rows of L_SS⁻¹ and of (L_SS⁻¹)ᵀ
   std::vector<int32_t> lvlRowPtr, lvlRows; // rows grouped by supernode level (leaves = level 0)
+
+  // Mixed precision: FP32 copies of the factor values, the dense inverses and D⁻¹, and Ã in
+  // elimination order (rows and columns permuted) for the FP64 refinement residual b − Ã·x.
+  std::vector<float> rowval32, colval32, invL32, invLT32, dinv32;
+  std::vector<int32_t> Aptr, Acol;
+  std::vector<double> Aval;
 };
 
 // Nested-dissection tree produced with an ordering: supernode ranges in elimination order.
@@ -93,6 +99,13 @@ void buildSupernodal(Factor& f, const SupernodeTree& tree);
 // instruction occupies its SMSP's pipe for ~80 cycles whatever its active lanes, so narrow groups
 // waste fewer lanes while wide groups spread a level's few long rows over more SMSPs.
 std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas);
+// The same for an FP32 solve run by one CTA of `ctaThreads` threads, where latency dominates.
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads);
+// Fills the mixed-precision fields of a factorized Factor (needs the supernodal fields).
+void buildMixed(Factor& f, const ScalarMatrix& A);
+// Explicit inverse Ã⁻¹ in vertex order, FP32, rows padded to `ld` (a multiple of 32) entries:
+// computed column by column with the FP64 factor (Ã is symmetric, so columns are rows).
+std::vector<float> denseInverse32(const Factor& f, int* ld);
 // Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
 bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
 void buildSchedules(Factor& f);

@@ -49,6 +49,30 @@ __device__ __forceinline__ double teamMax(const Team<CLUSTER>& tm, double v, dou
   return m;
 }
 
+// d_e = ℓ·rel/‖rel‖ (0 when degenerate), in FP64 or — with proj32 — in FP32 from the FP64
+// difference (the projection is where FP32 is safe: it only normalises a short vector).
+__device__ __forceinline__ void projectEdge(const InstanceDev& I, int e, double rx, double ry, double rz, double& dx,
+                                            double& dy, double& dz) {
+  if (I.proj32) {
+    const float fx = static_cast<float>(rx), fy = static_cast<float>(ry), fz = static_cast<float>(rz);
+    const float len = sqrtf(fx * fx + fy * fy + fz * fz);
+    if (!(len <= 1e-12f)) {
+      const float s = static_cast<float>(I.erest[e]) / len;
+      dx = fx * s;
+      dy = fy * s;
+      dz = fz * s;
+    }
+    return;
+  }
+  const double len = sqrt(rx * rx + ry * ry + rz * rz);
+  if (!(len <= 1e-12)) {
+    const double s = I.erest[e] / len;
+    dx = rx * s;
+    dy = ry * s;
+    dz = rz * s;
+  }
+}
+
 // Edge e at the current positions: κ·d_e and κ·rel − κ·d_e (DistanceTerm.cpp:94-152,
 // Integrator.cpp:246-248).
 template <bool CLUSTER>
@@ -57,14 +81,8 @@ __device__ __forceinline__ void edgeTerms(const InstanceDev& I, const Team<CLUST
   const double rx = tm.ld(I.x + 3 * a) - tm.ld(I.x + 3 * b);
   const double ry = tm.ld(I.x + 3 * a + 1) - tm.ld(I.x + 3 * b + 1);
   const double rz = tm.ld(I.x + 3 * a + 2) - tm.ld(I.x + 3 * b + 2);
-  const double len = sqrt(rx * rx + ry * ry + rz * rz);
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  if (!(len <= 1e-12)) {
-    const double s = I.erest[e] / len;
-    dx = rx * s;
-    dy = ry * s;
-    dz = rz * s;
-  }
+  projectEdge(I, e, rx, ry, rz, dx, dy, dz);
   const double k = I.ek[e];
   const double cx = dx * k, cy = dy * k, cz = dz * k;
   I.kd[3 * e] = cx;
@@ -191,6 +209,7 @@ struct TeamSolve {
     __device__ void accumulate(int idx, int lane, int G, double& a0, double& a1, double& a2) const {
       if (idx >= cnt) return;
       const int i = I.lvlRows[beg + idx];
+#pragma unroll 4
       for (int p = I.Lrp[i] + lane; p < I.offEnd[i]; p += G) {
         const int j = I.Lci[p];
         const double lv = I.Lrv[p];
@@ -216,6 +235,7 @@ struct TeamSolve {
       const int s0 = I.snStart[s];
       const int r = i - s0;
       const double* X = I.invL + I.snInvOff[s] + (int64_t)r * (r + 1) / 2;
+#pragma unroll 4
       for (int c = lane; c <= r; c += G) {
         const double xv = X[c];
         const int j = s0 + c;
@@ -237,6 +257,7 @@ struct TeamSolve {
     __device__ void accumulate(int idx, int lane, int G, double& a0, double& a1, double& a2) const {
       if (idx >= cnt) return;
       const int k = I.lvlRows[beg + idx];
+#pragma unroll 4
       for (int p = I.offBeg[k] + lane; p < I.Lcp[k + 1]; p += G) {
         const int i = I.Lri[p];
         const double lv = I.Lcv[p];
@@ -264,6 +285,7 @@ struct TeamSolve {
       const int sz = I.snStart[s + 1] - s0;
       const int r = k - s0;
       const double* XT = I.invLT + I.snInvOff[s] + (int64_t)r * sz - (int64_t)r * (r - 1) / 2;
+#pragma unroll 4
       for (int c = lane; c < sz - r; c += G) {
         const double xv = XT[c];
         const int j = k + c;
