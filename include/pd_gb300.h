@@ -46,7 +46,8 @@ extern "C" {
 #define PD_PRECISION_FP64 1       /* FP64, supernodal solve (reordered sums, FMA); matches to rounding */
 #define PD_PRECISION_FP32_PROJECTION 2 /* projection in FP32 accumulated into an FP64 b; FP64 solve */
 #define PD_PRECISION_FP32_SOLVE 3 /* FP32 supernodal solve + one FP64 iterative-refinement step */
-#define PD_PRECISION_MIXED 4      /* FP32 projection and FP32 solve + one FP64 refinement step */
+#define PD_PRECISION_MIXED 4      /* FP32 projection and FP32 solve + one FP64 refinement step; small
+                                     cloths: FP32 correction b − Ã·x and FP32 inverse, FP64 positions */
 
 /* Mirror of SceneConfig (core/sim/Scene.h:14-137) plus the fields the synthetic scenes need. */
 typedef struct pd_scene_config {
@@ -71,9 +72,10 @@ typedef struct pd_scene_config {
   int32_t pin_mode;          /* 0: corners of row ny-1 (reference default); 1: corners of row 0;
                                 2: whole row ny-1; 3: corner (0, ny-1); 4: none */
   int32_t precision;         /* PD_PRECISION_* */
-  int32_t cluster_ctas;      /* PD_PRECISION_FP64: CTAs sharing one cloth (1..16, a thread-block
-                                cluster); 0 = automatic (16 for up to 9 cloths, fewer for larger
-                                batches, 1 = one CTA per cloth) */
+  int32_t cluster_ctas;      /* CTAs sharing one cloth: a thread-block cluster (1..16) for the
+                                supernodal and FP32_SOLVE dense kernels, a team of co-resident CTAs
+                                (up to the SM count) for the MIXED dense kernel; 0 = automatic
+                                (the SMs shared out over the cloths), 1 = one CTA per cloth */
   int32_t dense_max_vertices; /* FP32_SOLVE / MIXED with a cluster: solve with the explicit FP32
                                  inverse of Ã when every cloth has at most this many vertices
                                  (0 = PD_DENSE_DEFAULT_MAX_VERTICES, < 0 = never) */
@@ -172,6 +174,8 @@ typedef struct pd_sim_info {
 #define PD_SOLVE_SUPERNODAL 1    /* FP64 nested-dissection supernodes */
 #define PD_SOLVE_SUPERNODAL32 2  /* FP32 supernodes + one FP64 refinement step */
 #define PD_SOLVE_DENSE32 3       /* explicit FP32 inverse + one FP64 refinement step */
+#define PD_SOLVE_DENSE32_TEAM 4  /* MIXED: explicit FP32 inverse applied to the correction b − Ã·x
+                                    by a team of co-resident CTAs per cloth (FP64 positions) */
 
 typedef struct pd_sim_stats {    /* SimContext counters (core/sim/Scene.h:161-169) */
   int32_t iterations_used;       /* of the last substep */

@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     PD_SOLVE_SUPERNODAL,
     PD_SOLVE_SUPERNODAL32,
     PD_SOLVE_DENSE32,
+    PD_SOLVE_DENSE32_TEAM,
     PdError,
     SceneConfig,
     GridScene,

@@ -25,6 +25,7 @@ PD_SOLVE_LEVELS = 0               # solve kinds reported by Simulator.info()["so
 PD_SOLVE_SUPERNODAL = 1
 PD_SOLVE_SUPERNODAL32 = 2
 PD_SOLVE_DENSE32 = 3
+PD_SOLVE_DENSE32_TEAM = 4
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpd_gb300.so")

@@ -24,6 +24,7 @@ UNITS = {
     "substep_exact.cu": ["-fmad=false"],
     "substep_fast.cu": [],
     "substep_mixed.cu": [],
+    "substep_delta.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
 }
 

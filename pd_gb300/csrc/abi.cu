@@ -93,8 +93,9 @@ struct Instance {
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
       oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
-      oVptr, oVcol, oVval;
-  int denseLd = 0;  // > 0: Ã⁻¹ is in the arena
+      oVptr, oVcol, oVval, oXbuf, oRbuf, oPart, oBar, oErr, oEdge32, oBfac32, oVtx32;
+  int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
+  int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
   size_t bytes = 0;
 };
 
@@ -131,19 +132,62 @@ std::string prepare(Instance& I, bool reanalyze) {
   return {};
 }
 
-void layout(Instance& I, Arena& A, int teamCtas, bool dense) {
+// Shared memory of the team kernel for one instance: positions as hi/lo pairs (32 B a vertex),
+// the padded correction (12 B a row), `resRows` rows of Ã⁻¹, and per owned vertex x, x_n, x̂, v
+// (FP64) and Δ (FP32). Fills *resRows with as many rows as fit in kDeltaSmem (even unless all).
+constexpr int kDeltaSmem = 220 * 1024;
+int deltaSmem(int n, int team, int* resRows) {
+  const int ld = (n + 31) / 32 * 32, chunk = (n + team - 1) / team;
+  const long fixed = 32L * n + 12L * ld + 108L * chunk;
+  long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (4L * ld) : 0;
+  if (rows >= chunk) {
+    rows = chunk;
+  } else {
+    rows &= ~1L;
+  }
+  *resRows = static_cast<int>(rows);
+  return static_cast<int>(fixed + 4L * rows * ld);
+}
+
+// kind: 0 none, 1 dense inverse (cluster kernel), 2 dense inverse + team kernel buffers
+void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
   I.oLvlG = A.add(pdg::chooseGroupWidths(I.F, teamCtas));
+  const size_t before = A.host.size();
   I.denseLd = 0;
+  I.denseResRows = 0;
   I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
-  if (dense) {
+  I.oXbuf = I.oRbuf = I.oPart = I.oBar = I.oErr = I.oEdge32 = I.oBfac32 = I.oVtx32 = 0;
+  if (denseKind > 0) {
     I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
     I.oVcol = A.add(I.L.col);
     I.oVval = A.add(I.L.val);
   }
-  const size_t before = A.host.size();
+  if (denseKind == 2) {
+    deltaSmem(s.n, teamCtas, &I.denseResRows);
+    I.oXbuf = A.zeros(32 * n);
+    I.oRbuf = A.zeros(12 * static_cast<size_t>(I.denseLd));
+    I.oPart = A.zeros(sizeof(double) * 6 * teamCtas);
+    I.oBar = A.zeros(8);
+    I.oErr = A.zeros(4);
+    std::vector<float> e32(2 * ne), b32(I.topo.bfac.size()), v32(2 * n);
+    for (size_t e = 0; e < ne; ++e) {
+      e32[2 * e] = static_cast<float>(s.edges[e].rest);
+      e32[2 * e + 1] = static_cast<float>(s.edges[e].k);
+    }
+    for (size_t q = 0; q < b32.size(); ++q) b32[q] = static_cast<float>(I.topo.bfac[q]);
+    const double invH2 = 1.0 / (I.cfg.dt * I.cfg.dt);
+    for (size_t v = 0; v < n; ++v) {
+      const double mv = s.m[v];
+      v32[2 * v] = static_cast<float>(mv * invH2);
+      v32[2 * v + 1] = mv > 0.0 ? static_cast<float>(1.0 / mv) : 0.0f;
+    }
+    I.oEdge32 = A.add(e32);
+    I.oBfac32 = A.add(b32);
+    I.oVtx32 = A.add(v32);
+  }
   I.oX = A.add(s.x);
   I.oV = A.add(s.v);
   I.oXn = A.zeros(24 * n);
@@ -313,6 +357,17 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
     d.Vcol = reinterpret_cast<const int32_t*>(P(I.oVcol));
     d.Vval = reinterpret_cast<const double*>(P(I.oVval));
   }
+  d.denseResRows = I.denseResRows;
+  if (I.oXbuf) {
+    d.xbuf = reinterpret_cast<float*>(P(I.oXbuf));
+    d.rbuf = reinterpret_cast<float*>(P(I.oRbuf));
+    d.part = reinterpret_cast<double*>(P(I.oPart));
+    d.bar = reinterpret_cast<unsigned long long*>(P(I.oBar));
+    d.err = reinterpret_cast<int32_t*>(P(I.oErr));
+    d.edge32 = reinterpret_cast<const float*>(P(I.oEdge32));
+    d.bfac32 = reinterpret_cast<const float*>(P(I.oBfac32));
+    d.vtx32 = reinterpret_cast<const float*>(P(I.oVtx32));
+  }
   d.iterLog = iterLog;
   d.convLog = convLog;
   d.lastResidual = reinterpret_cast<double*>(P(I.oLastRes));
@@ -347,6 +402,7 @@ struct pd_sim {
   int smemBytes = 0;
   int teamCtas = 1;  // CTAs per instance (a thread-block cluster when > 1)
   bool dense = false;  // mixed modes: the cluster applies the explicit FP32 inverse
+  bool delta = false;  // MIXED: a team of co-resident CTAs per cloth, correction-form dense solve
 
   ~pd_sim() { release(); }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
@@ -363,7 +419,9 @@ struct pd_sim {
     const int p = precision();
     teamCtas = 1;
     dense = false;
+    delta = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
+    if (p == PD_PRECISION_MIXED && planDelta()) return;
     int want = inst[0].cfg.cluster_ctas;
     if (want <= 0) {
       const int count = static_cast<int>(inst.size());
@@ -391,6 +449,33 @@ struct pd_sim {
     while (cs > 1 && pdg::mixedClusterSupported(cs, 72 * maxN) != cs) cs /= 2;
     teamCtas = cs;
   }
+  // MIXED with every cloth small enough for the explicit inverse: `cluster_ctas` CTAs per cloth
+  // (0: the SMs shared out over the cloths), all co-resident, at most one per vertex.
+  bool planDelta() {
+    int maxN = 0, minN = 1 << 30;
+    for (const auto& I : inst) {
+      maxN = std::max(maxN, I.scene.n);
+      minN = std::min(minN, I.scene.n);
+    }
+    if (maxN > denseLimit()) return false;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const int count = static_cast<int>(inst.size());
+    const int want = inst[0].cfg.cluster_ctas;
+    int team = want > 0 ? want : sms / count;
+    team = std::min({team, sms / count, minN});
+    if (team < 2) return false;
+    int smem = 0, rows = 0;
+    for (const auto& I : inst) smem = std::max(smem, deltaSmem(I.scene.n, team, &rows));
+    if (pdg::deltaResidentCtas(smem) < count * team) return false;
+    teamCtas = team;
+    delta = true;
+    return true;
+  }
   // Largest cloth solved with the explicit inverse: the configured limit, capped by the
   // kernel's shared memory (denseSmem(n) ≤ kMaxSmem).
   int denseLimit() const {
@@ -415,7 +500,7 @@ struct pd_sim {
   int upload(int capacity) {
     Arena A;
     planTeam();
-    for (auto& I : inst) layout(I, A, teamCtas, dense);
+    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : dense ? 1 : 0);
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -444,8 +529,11 @@ struct pd_sim {
     for (size_t i = 0; i < inst.size(); ++i) {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
-      const int need = dense ? denseSmem(inst[i].scene.n) : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
-      if (need <= kMaxSmem && need > smem) smem = need;
+      int rows = 0;
+      const int need = delta   ? deltaSmem(inst[i].scene.n, teamCtas, &rows)
+                       : dense ? denseSmem(inst[i].scene.n)
+                               : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
+      if ((delta || need <= kMaxSmem) && need > smem) smem = need;
     }
     smemBytes = smem;
     if (!dDesc) PD_CUDA(cudaMalloc(&dDesc, sizeof(pdg::InstanceDev) * inst.size()));
@@ -454,8 +542,27 @@ struct pd_sim {
   }
 
   // Copies device positions / velocities of every instance back into the host scenes.
-  int pullState() {
+  // Waits for the stream; a team barrier that gave up waiting is reported here (and the
+  // barrier counters are reset so that later launches start clean).
+  int sync() {
     PD_CUDA(cudaStreamSynchronize(stream));
+    if (!delta) return PD_OK;
+    int bad = 0;
+    for (const auto& I : inst) {
+      int32_t e = 0;
+      PD_CUDA(cudaMemcpy(&e, dArena + I.oErr, 4, cudaMemcpyDeviceToHost));
+      bad |= e;
+    }
+    if (!bad) return PD_OK;
+    for (const auto& I : inst) {
+      PD_CUDA(cudaMemset(dArena + I.oErr, 0, 4));
+      PD_CUDA(cudaMemset(dArena + I.oBar, 0, 8));
+    }
+    return fail(PD_ERR_CUDA, "a team barrier of the substep kernel gave up waiting; the state is undefined");
+  }
+
+  int pullState() {
+    if (const int rc_ = sync()) return rc_;
     for (auto& I : inst) {
       PD_CUDA(cudaMemcpy(I.scene.x.data(), dArena + I.oX, 24 * I.scene.n, cudaMemcpyDeviceToHost));
       PD_CUDA(cudaMemcpy(I.scene.v.data(), dArena + I.oV, 24 * I.scene.n, cudaMemcpyDeviceToHost));
@@ -714,7 +821,7 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
   if (substeps < 0) return fail(PD_ERR_INVALID_ARGUMENT, "substeps must be >= 0");
   if (substeps == 0) return PD_OK;
   if (substeps > s->logCapacity) {
-    PD_CUDA(cudaStreamSynchronize(s->stream));
+    if (const int rc_ = s->sync()) return rc_;
     const int rc = s->ensureLogs(substeps);
     if (rc != PD_OK) return rc;
   }
@@ -723,6 +830,8 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
   const int p = s->precision();
   if (p == PD_PRECISION_FP64_EXACT) {
     rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
+  } else if (s->delta) {
+    rc = pdg::launchSubstepDelta(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (s->dense) {
     rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (mixedSolve(p)) {
@@ -739,7 +848,7 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
 
 int pd_sim_synchronize(pd_sim* s) {
   if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   return PD_OK;
 }
 
@@ -756,7 +865,7 @@ int pd_sim_get_state(pd_sim* s, int32_t i, double* x, double* v) {
   const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
   if (x) PD_CUDA(cudaMemcpyAsync(x, s->dArena + I.oX, bytes, cudaMemcpyDeviceToHost, s->stream));
   if (v) PD_CUDA(cudaMemcpyAsync(v, s->dArena + I.oV, bytes, cudaMemcpyDeviceToHost, s->stream));
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   return PD_OK;
 }
 
@@ -801,7 +910,7 @@ int pd_sim_set_pin_positions(pd_sim* s, int32_t i, const double* q) {
   pdg::assembleBendingRhs(I.scene, I.bendRhs);
   PD_CUDA(cudaMemcpyAsync(s->dArena + I.oQ, I.scene.q.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
   PD_CUDA(cudaMemcpyAsync(s->dArena + I.oBend, I.bendRhs.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   return PD_OK;
 }
 
@@ -855,7 +964,7 @@ int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
     }
     return s->upload(s->logCapacity);
   }
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   return s->writeDescriptors();
 }
 
@@ -879,6 +988,7 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   const int p = s->precision();
   out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                     : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
+                    : s->delta                   ? PD_SOLVE_DENSE32_TEAM
                     : s->dense                   ? PD_SOLVE_DENSE32
                                                  : PD_SOLVE_SUPERNODAL32;
   return PD_OK;
@@ -889,7 +999,7 @@ int pd_sim_get_stats(pd_sim* s, int32_t i, pd_sim_stats* out) {
   if (rc) return rc;
   if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
   const Instance& I = s->inst[i];
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   int32_t ints[3];
   PD_CUDA(cudaMemcpy(&out->last_residual, s->dArena + I.oLastRes, sizeof(double), cudaMemcpyDeviceToHost));
   PD_CUDA(cudaMemcpy(&ints[0], s->dArena + I.oIters, 4, cudaMemcpyDeviceToHost));
@@ -905,7 +1015,7 @@ int pd_sim_iteration_log(pd_sim* s, int32_t i, int32_t* iters, uint8_t* conv, in
   int rc = checkInstance(s, i);
   if (rc) return rc;
   if (count < 0 || count > s->lastSubsteps) return fail(PD_ERR_INVALID_ARGUMENT, "count exceeds the last step's substeps");
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   if (iters) PD_CUDA(cudaMemcpy(iters, s->dIterLog + static_cast<size_t>(i) * s->logCapacity, 4 * count, cudaMemcpyDeviceToHost));
   if (conv) PD_CUDA(cudaMemcpy(conv, s->dConvLog + static_cast<size_t>(i) * s->logCapacity, count, cudaMemcpyDeviceToHost));
   return PD_OK;
@@ -945,7 +1055,7 @@ int pd_sim_solve(pd_sim* s, int32_t i, const double* b, double* x) {
     return cudaFail(static_cast<cudaError_t>(lrc), "solve launch");
   }
   PD_CUDA(cudaMemcpyAsync(x, dX, bytes, cudaMemcpyDeviceToHost, s->stream));
-  PD_CUDA(cudaStreamSynchronize(s->stream));
+  if (const int rc_ = s->sync()) return rc_;
   PD_CUDA(cudaFree(dB));
   return PD_OK;
 }
@@ -971,7 +1081,7 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
   if (dinv) std::memcpy(dinv, F.dinv.data(), F.dinv.size() * 8);
   if (info) {
     Arena A;
-    layout(I, A, 1, false);
+    layout(I, A, 1, 0);
     info->cluster_ctas = 1;
     info->solve_kind = I.cfg.precision == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                        : mixedSolve(I.cfg.precision)              ? PD_SOLVE_SUPERNODAL32

@@ -95,6 +95,16 @@ struct InstanceDev {
   const int32_t* Vptr;
   const int32_t* Vcol;
   const double* Vval;
+  // correction-form dense solve by a team of CTAs (MIXED): exchange buffers in L2, team barrier
+  int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (even)
+  float* xbuf;                 // 8n: per vertex (hi x, y, z, 0, lo x, y, z, 0), x = hi + lo
+  float* rbuf;                 // 3·denseLd: correction b − Ã·x, one padded array per component
+  double* part;                // 2 × team × 3: per-CTA maxima (residual, displacement, scale)
+  unsigned long long* bar;     // team barrier arrivals (monotonic)
+  int32_t* err;                // set when a team barrier gave up waiting
+  const float* edge32;         // 2E: rest length, κ
+  const float* bfac32;         // (−k)·w_v per bend incidence
+  const float* vtx32;          // 2n: m/h², 1/m (0 when m ≤ 0)
   // statistics
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;
@@ -129,6 +139,12 @@ int mixedClusterSupported(int clusterSize, int smemBytes);
 int launchSubstepDenseCluster(const InstanceDev* dInstances, int count, int clusterSize, int smemBytes, int substeps,
                               void* stream);
 int denseClusterSupported(int clusterSize, int smemBytes);
+// MIXED substep for small cloths by `team` co-resident CTAs per instance (cooperative launch):
+// x ← x + Ã⁻¹·(b − Ã·x) with the rows of the explicit FP32 inverse split over the team.
+int launchSubstepDelta(const InstanceDev* dInstances, int count, int team, int smemBytes, int substeps, void* stream);
+// CTAs of kDeltaThreads threads with smemBytes each that can be co-resident on the device.
+int deltaResidentCtas(int smemBytes);
+constexpr int kDeltaThreads = 512;
 
 constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per

@@ -19,8 +19,9 @@ MODES = {"fp32-projection": 2, "fp32-solve": 3, "mixed": 4}
 
 
 # (CTAs per cloth, dense_max_vertices): one CTA; a cluster whose CTAs each run the supernodal
-# FP32 solve; a cluster splitting the rows of the explicit FP32 inverse
-STRATEGIES = {"one-cta": (1, 0), "cluster-supernodal": (16, -1), "cluster-dense": (16, 0)}
+# FP32 solve; 16 CTAs splitting the rows of the explicit FP32 inverse (a cluster for FP32_SOLVE,
+# a team with the correction-form solve for MIXED); every SM on the cloth (MIXED team)
+STRATEGIES = {"one-cta": (1, 0), "cluster-supernodal": (16, -1), "cluster-dense": (16, 0), "auto": (0, 0)}
 
 
 def with_mode(cfg, mode, ctas=0, dense=0):
@@ -34,7 +35,9 @@ def with_mode(cfg, mode, ctas=0, dense=0):
 def expected_kind(pdg, mode, ctas, dense):
     if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION:
         return pdg.PD_SOLVE_SUPERNODAL
-    return pdg.PD_SOLVE_DENSE32 if (ctas > 1 and dense >= 0) else pdg.PD_SOLVE_SUPERNODAL32
+    if ctas == 1 or dense < 0:
+        return pdg.PD_SOLVE_SUPERNODAL32
+    return pdg.PD_SOLVE_DENSE32_TEAM if MODES[mode] == pdg.PD_PRECISION_MIXED else pdg.PD_SOLVE_DENSE32
 
 
 @pytest.mark.parametrize("mode", list(MODES))
@@ -42,7 +45,7 @@ def expected_kind(pdg, mode, ctas, dense):
 def test_plain_cloth_600_substeps(pdg, mode, strategy):
     scenes, cfg, substeps = W.cloth40_plain()
     ctas, dense = STRATEGIES[strategy]
-    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION and strategy == "cluster-dense":
+    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION and strategy in ("cluster-dense", "auto"):
         pytest.skip("the FP64 solve has no dense variant")
     sim = pdg.Simulator(scenes[0], with_mode(cfg, mode, ctas, dense))
     assert sim.info()["solve_kind"] == expected_kind(pdg, mode, ctas, dense)
@@ -94,3 +97,68 @@ def test_large_cloth_uses_global_workspace(pdg):
     sim.step(30)
     orc.step(30)
     assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
+
+
+@pytest.mark.parametrize("strategy", ["cluster-dense", "auto"])
+def test_team_pin_move(pdg, strategy):
+    """Handles dragged between steps: the first iterate's matrix couples neighbours at the new q
+    while the projections still see the old pin positions."""
+    scenes, cfg, _ = W.cloth40_plain()
+    scene = scenes[0]
+    ctas, dense = STRATEGIES[strategy]
+    sim = pdg.Simulator(scene, with_mode(cfg, "mixed", ctas, dense))
+    assert sim.info()["solve_kind"] == pdg.PD_SOLVE_DENSE32_TEAM
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    pins = np.flatnonzero(scene.pinned)
+    sim.step(20)
+    orc.step(20)
+    q = scene.positions.copy()
+    q[pins, 0] += 0.05
+    q[pins, 2] -= 0.03
+    sim.set_pin_positions(q)
+    orc.set_pin_positions(q)
+    for _ in range(3):
+        sim.step(20)
+        orc.step(20)
+        assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
+    x, v = sim.state()
+    assert np.array_equal(x[pins], q[pins]) and not np.any(v[pins])
+
+
+def test_team_gates(pdg):
+    """Team kernel: residual gate that fires, displacement gate, and zero iterations."""
+    cases = [
+        W._base(grid_nx=12, grid_ny=12, grid_spacing=0.05, max_iterations=30, residual_tolerance=0.3,
+                velocity_damping=0.02),
+        W._base(grid_nx=10, grid_ny=14, grid_spacing=0.05, max_iterations=25, residual_tolerance=0.0,
+                rel_tolerance=5e-2),
+        W._base(grid_nx=10, grid_ny=10, grid_spacing=0.05, max_iterations=0),
+    ]
+    for cfg in cases:
+        scene = pdg.make_grid(cfg)
+        sim = pdg.Simulator(scene, with_mode(cfg, "mixed"))
+        assert sim.info()["solve_kind"] == pdg.PD_SOLVE_DENSE32_TEAM
+        orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+        sim.step(100)
+        it_o, cv_o = orc.step(100)
+        it_g, cv_g = sim.iteration_log()
+        assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
+        assert np.mean(it_g == it_o) > 0.95 and np.mean(cv_g == cv_o) > 0.95
+        st = sim.stats()
+        if cfg.max_iterations == 0:
+            assert st["iterations_used"] == 0 and not np.any(it_g)
+
+
+def test_team_batch_and_repeated_launches(pdg):
+    """Several cloths share the SMs; many short launches reuse the team barrier counters."""
+    scenes, cfgs, _ = W.batch(count=6, seed=91, max_side=40)
+    sim = pdg.Simulator(scenes, [with_mode(c, "mixed") for c in cfgs])
+    assert sim.info()["solve_kind"] == pdg.PD_SOLVE_DENSE32_TEAM
+    assert sim.info()["cluster_ctas"] >= 2
+    for _ in range(25):
+        sim.step(2)
+    sim.synchronize()
+    for i, (s, c) in enumerate(zip(scenes, cfgs)):
+        orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
+        orc.step(50)
+        assert max_rel(sim.state(i)[0], orc.state()[0]) < TOL_POS, i
