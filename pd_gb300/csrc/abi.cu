@@ -93,9 +93,10 @@ struct Instance {
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
       oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
-      oVptr, oVcol, oVval, oXbuf, oRbuf, oPart, oBar, oErr, oEdge32, oBfac32, oVtx32;
+      oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl;
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
+  int teamECap = 0, teamBCap = 0;
   size_t bytes = 0;
 };
 
@@ -136,9 +137,39 @@ std::string prepare(Instance& I, bool reanalyze) {
 // the padded correction (12 B a row), `resRows` rows of Ã⁻¹, and per owned vertex x, x_n, x̂, v
 // (FP64) and Δ (FP32). Fills *resRows with as many rows as fit in kDeltaSmem (even unless all).
 constexpr int kDeltaSmem = 220 * 1024;
-int deltaSmem(int n, int team, int* resRows) {
-  const int ld = (n + 31) / 32 * 32, chunk = (n + team - 1) / team;
-  const long fixed = 32L * n + 12L * ld + 108L * chunk;
+// Pin positions as FP32 pairs per vertex: hi (x, y, z, 0), lo (x, y, z, 0) with hi = fl32(q) and
+// lo = fl32(q − hi), the split the team kernel applies to positions.
+std::vector<float> pinPairs(const pdg::Scene& s) {
+  std::vector<float> out(8 * static_cast<size_t>(s.n), 0.0f);
+  for (size_t v = 0; v < static_cast<size_t>(s.n); ++v) {
+    for (int c = 0; c < 3; ++c) {
+      const double q = s.q[3 * v + c];
+      const float hi = static_cast<float>(q);
+      out[8 * v + c] = hi;
+      out[8 * v + 4 + c] = static_cast<float>(q - static_cast<double>(hi));
+    }
+  }
+  return out;
+}
+
+// Most edge / bend incidences of one CTA's vertex range.
+void teamCaps(const Instance& I, int team, int* eCap, int* bCap) {
+  const int n = I.scene.n, chunk = (n + team - 1) / team;
+  *eCap = *bCap = 0;
+  for (int r = 0; r < team; ++r) {
+    const int rb = std::min(n, r * chunk), re = std::min(n, rb + chunk);
+    *eCap = std::max(*eCap, I.topo.rstart[re] - I.topo.rstart[rb]);
+    *bCap = std::max(*bCap, I.topo.bstart[re] - I.topo.bstart[rb]);
+  }
+}
+
+int deltaSmem(const Instance& I, int team, int* resRows) {
+  const int n = I.scene.n, ld = (n + 31) / 32 * 32, chunk = (n + team - 1) / team;
+  int eCap = 0, bCap = 0;
+  teamCaps(I, team, &eCap, &bCap);
+  // positions, correction, incidences, vertex constants, FP64 state, Δ, incidence offsets
+  // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 48·chunk partial sums of Δ)
+  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 144L * chunk + 8L * (chunk + 1);
   long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (4L * ld) : 0;
   if (rows >= chunk) {
     rows = chunk;
@@ -158,7 +189,8 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.denseLd = 0;
   I.denseResRows = 0;
   I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
-  I.oXbuf = I.oRbuf = I.oPart = I.oBar = I.oErr = I.oEdge32 = I.oBfac32 = I.oVtx32 = 0;
+  I.oRtag = I.oXtag = I.oPtag = I.oEpoch = I.oWindow = I.oErr = I.oTEdge = I.oTBend = I.oTVtx = I.oQhl = 0;
+  I.teamECap = I.teamBCap = 0;
   if (denseKind > 0) {
     I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
@@ -166,27 +198,72 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
     I.oVval = A.add(I.L.val);
   }
   if (denseKind == 2) {
-    deltaSmem(s.n, teamCtas, &I.denseResRows);
-    I.oXbuf = A.zeros(32 * n);
-    I.oRbuf = A.zeros(12 * static_cast<size_t>(I.denseLd));
-    I.oPart = A.zeros(sizeof(double) * 6 * teamCtas);
-    I.oBar = A.zeros(8);
+    deltaSmem(I, teamCtas, &I.denseResRows);
+    teamCaps(I, teamCtas, &I.teamECap, &I.teamBCap);
+    I.oRtag = A.zeros(8 * 3 * n);
+    I.oXtag = A.zeros(8 * 6 * n);
+    I.oPtag = A.zeros(8 * 2 * 16 * static_cast<size_t>(teamCtas));  // one 128-byte line per partial
+    I.oEpoch = A.zeros(4);
     I.oErr = A.zeros(4);
-    std::vector<float> e32(2 * ne), b32(I.topo.bfac.size()), v32(2 * n);
-    for (size_t e = 0; e < ne; ++e) {
-      e32[2 * e] = static_cast<float>(s.edges[e].rest);
-      e32[2 * e + 1] = static_cast<float>(s.edges[e].k);
+    // positions a CTA reads: its vertices, their edge neighbours and bend-stencil partners
+    std::vector<int32_t> window(2 * static_cast<size_t>(teamCtas), 0);
+    const int chunk = (s.n + teamCtas - 1) / teamCtas;
+    for (int r = 0; r < teamCtas; ++r) {
+      const int rb = std::min(s.n, r * chunk), re = std::min(s.n, rb + chunk);
+      if (rb >= re) continue;
+      int lo = rb, hi = re;
+      for (int v = rb; v < re; ++v) {
+        for (int q = I.topo.rstart[v]; q < I.topo.rstart[v + 1]; ++q) {
+          const pdg::Edge& e = s.edges[I.topo.rinc[q] >> 1];
+          lo = std::min({lo, e.a, e.b});
+          hi = std::max({hi, e.a + 1, e.b + 1});
+        }
+        for (int q = I.topo.bstart[v]; q < I.topo.bstart[v + 1]; ++q) {
+          const pdg::Bend& b = s.bends[I.topo.binc[q]];
+          lo = std::min({lo, b.a, b.b, b.c});
+          hi = std::max({hi, b.a + 1, b.b + 1, b.c + 1});
+        }
+      }
+      window[2 * r] = lo;
+      window[2 * r + 1] = hi;
     }
-    for (size_t q = 0; q < b32.size(); ++q) b32[q] = static_cast<float>(I.topo.bfac[q]);
+    I.oWindow = A.add(window);
+    // incidences in the kernel's FP32 form (pinned endpoints flagged in bit 31)
+    auto bitsOf = [](float f) {
+      int32_t i;
+      std::memcpy(&i, &f, 4);
+      return i;
+    };
+    auto flag = [&](int v) { return s.pinned[v] ? static_cast<int32_t>(0x80000000u | static_cast<uint32_t>(v)) : v; };
+    std::vector<int32_t> te(4 * I.topo.rinc.size()), tb(4 * I.topo.binc.size());
+    for (int v = 0; v < s.n; ++v) {
+      for (int q = I.topo.rstart[v]; q < I.topo.rstart[v + 1]; ++q) {
+        const pdg::Edge& e = s.edges[I.topo.rinc[q] >> 1];
+        const int o = (I.topo.rinc[q] & 1) ? e.a : e.b;
+        te[4 * q] = flag(o);
+        te[4 * q + 1] = bitsOf(static_cast<float>(e.rest));
+        te[4 * q + 2] = bitsOf(static_cast<float>(e.k));
+      }
+      for (int q = I.topo.bstart[v]; q < I.topo.bstart[v + 1]; ++q) {
+        const pdg::Bend& b = s.bends[I.topo.binc[q]];
+        tb[4 * q] = flag(b.a);
+        tb[4 * q + 1] = flag(b.b);
+        tb[4 * q + 2] = flag(b.c);
+        tb[4 * q + 3] = bitsOf(static_cast<float>(I.topo.bfac[q]));
+      }
+    }
+    std::vector<float> tv(4 * n, 0.0f);
     const double invH2 = 1.0 / (I.cfg.dt * I.cfg.dt);
     for (size_t v = 0; v < n; ++v) {
       const double mv = s.m[v];
-      v32[2 * v] = static_cast<float>(mv * invH2);
-      v32[2 * v + 1] = mv > 0.0 ? static_cast<float>(1.0 / mv) : 0.0f;
+      tv[4 * v] = static_cast<float>(mv * invH2);
+      tv[4 * v + 1] = mv > 0.0 ? static_cast<float>(1.0 / mv) : 0.0f;
+      tv[4 * v + 2] = s.pinned[v] ? 1.0f : 0.0f;
     }
-    I.oEdge32 = A.add(e32);
-    I.oBfac32 = A.add(b32);
-    I.oVtx32 = A.add(v32);
+    I.oTEdge = A.add(te);
+    I.oTBend = A.add(tb);
+    I.oTVtx = A.add(tv);
+    I.oQhl = A.add(pinPairs(s));
   }
   I.oX = A.add(s.x);
   I.oV = A.add(s.v);
@@ -358,15 +435,19 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
     d.Vval = reinterpret_cast<const double*>(P(I.oVval));
   }
   d.denseResRows = I.denseResRows;
-  if (I.oXbuf) {
-    d.xbuf = reinterpret_cast<float*>(P(I.oXbuf));
-    d.rbuf = reinterpret_cast<float*>(P(I.oRbuf));
-    d.part = reinterpret_cast<double*>(P(I.oPart));
-    d.bar = reinterpret_cast<unsigned long long*>(P(I.oBar));
+  if (I.oRtag) {
+    d.teamECap = I.teamECap;
+    d.teamBCap = I.teamBCap;
+    d.tEdge = reinterpret_cast<const int4*>(P(I.oTEdge));
+    d.tBend = reinterpret_cast<const int4*>(P(I.oTBend));
+    d.tVtx = reinterpret_cast<const float4*>(P(I.oTVtx));
+    d.qhl = reinterpret_cast<const float4*>(P(I.oQhl));
+    d.rtag = reinterpret_cast<unsigned long long*>(P(I.oRtag));
+    d.xtag = reinterpret_cast<unsigned long long*>(P(I.oXtag));
+    d.ptag = reinterpret_cast<unsigned long long*>(P(I.oPtag));
+    d.epoch = reinterpret_cast<uint32_t*>(P(I.oEpoch));
+    d.window = reinterpret_cast<const int32_t*>(P(I.oWindow));
     d.err = reinterpret_cast<int32_t*>(P(I.oErr));
-    d.edge32 = reinterpret_cast<const float*>(P(I.oEdge32));
-    d.bfac32 = reinterpret_cast<const float*>(P(I.oBfac32));
-    d.vtx32 = reinterpret_cast<const float*>(P(I.oVtx32));
   }
   d.iterLog = iterLog;
   d.convLog = convLog;
@@ -467,10 +548,10 @@ struct pd_sim {
     const int count = static_cast<int>(inst.size());
     const int want = inst[0].cfg.cluster_ctas;
     int team = want > 0 ? want : sms / count;
-    team = std::min({team, sms / count, minN});
+    team = std::min({team, sms / count, minN, 256});  // 256: flags one polling warp covers
     if (team < 2) return false;
     int smem = 0, rows = 0;
-    for (const auto& I : inst) smem = std::max(smem, deltaSmem(I.scene.n, team, &rows));
+    for (const auto& I : inst) smem = std::max(smem, deltaSmem(I, team, &rows));
     if (pdg::deltaResidentCtas(smem) < count * team) return false;
     teamCtas = team;
     delta = true;
@@ -530,7 +611,7 @@ struct pd_sim {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
       int rows = 0;
-      const int need = delta   ? deltaSmem(inst[i].scene.n, teamCtas, &rows)
+      const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
                        : dense ? denseSmem(inst[i].scene.n)
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       if ((delta || need <= kMaxSmem) && need > smem) smem = need;
@@ -556,9 +637,12 @@ struct pd_sim {
     if (!bad) return PD_OK;
     for (const auto& I : inst) {
       PD_CUDA(cudaMemset(dArena + I.oErr, 0, 4));
-      PD_CUDA(cudaMemset(dArena + I.oBar, 0, 8));
+      PD_CUDA(cudaMemset(dArena + I.oEpoch, 0, 4));
+      PD_CUDA(cudaMemset(dArena + I.oPtag, 0, 8 * 2 * 16 * static_cast<size_t>(teamCtas)));
+      PD_CUDA(cudaMemset(dArena + I.oRtag, 0, 8 * 3 * static_cast<size_t>(I.scene.n)));
+      PD_CUDA(cudaMemset(dArena + I.oXtag, 0, 8 * 6 * static_cast<size_t>(I.scene.n)));
     }
-    return fail(PD_ERR_CUDA, "a team barrier of the substep kernel gave up waiting; the state is undefined");
+    return fail(PD_ERR_CUDA, "a team exchange of the substep kernel gave up waiting; the state is undefined");
   }
 
   int pullState() {
@@ -910,6 +994,11 @@ int pd_sim_set_pin_positions(pd_sim* s, int32_t i, const double* q) {
   pdg::assembleBendingRhs(I.scene, I.bendRhs);
   PD_CUDA(cudaMemcpyAsync(s->dArena + I.oQ, I.scene.q.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
   PD_CUDA(cudaMemcpyAsync(s->dArena + I.oBend, I.bendRhs.data(), 24 * static_cast<size_t>(I.scene.n), cudaMemcpyHostToDevice, s->stream));
+  std::vector<float> pairs;
+  if (I.oQhl) {
+    pairs = pinPairs(I.scene);
+    PD_CUDA(cudaMemcpyAsync(s->dArena + I.oQhl, pairs.data(), 4 * pairs.size(), cudaMemcpyHostToDevice, s->stream));
+  }
   if (const int rc_ = s->sync()) return rc_;
   return PD_OK;
 }

@@ -95,16 +95,20 @@ struct InstanceDev {
   const int32_t* Vptr;
   const int32_t* Vcol;
   const double* Vval;
-  // correction-form dense solve by a team of CTAs (MIXED): exchange buffers in L2, team barrier
-  int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (even)
-  float* xbuf;                 // 8n: per vertex (hi x, y, z, 0, lo x, y, z, 0), x = hi + lo
-  float* rbuf;                 // 3·denseLd: correction b − Ã·x, one padded array per component
-  double* part;                // 2 × team × 3: per-CTA maxima (residual, displacement, scale)
-  unsigned long long* bar;     // team barrier arrivals (monotonic)
-  int32_t* err;                // set when a team barrier gave up waiting
-  const float* edge32;         // 2E: rest length, κ
-  const float* bfac32;         // (−k)·w_v per bend incidence
-  const float* vtx32;          // 2n: m/h², 1/m (0 when m ≤ 0)
+  // correction-form dense solve by a team of CTAs (MIXED). Exchange words carry
+  // (epoch << 32 | FP32 bits): a reader knows a word is current from its epoch alone.
+  int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (even unless all)
+  int32_t teamECap, teamBCap;  // most edge / bend incidences of one CTA's vertices
+  const int4* tEdge;           // per edge incidence (rstart order): other | pinned << 31, rest, κ (FP32 bits), 0
+  const int4* tBend;           // per bend incidence (bstart order): a, b, c (| pinned << 31), (−k)·w_v bits
+  const float4* tVtx;          // per vertex: m/h², 1/m (0 when m ≤ 0), pinned, 0
+  const float4* qhl;           // per vertex: pin position as hi (x, y, z, 0), lo (x, y, z, 0)
+  unsigned long long* rtag;    // 3n words: correction b − Ã·x, component-major
+  unsigned long long* xtag;    // 6n words: positions as hi x, y, z, lo x, y, z (x = hi + lo)
+  unsigned long long* ptag;    // 2 × team × 16 words: per-CTA partial maxima of the two exchanges
+  uint32_t* epoch;             // last exchange epoch of the previous launch
+  const int32_t* window;       // 2 × team: vertex range [lo, hi) whose positions a CTA reads
+  int32_t* err;                // set when an exchange gave up waiting
   // statistics
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;

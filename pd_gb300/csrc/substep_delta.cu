@@ -5,22 +5,31 @@
 //   x^{k+1} = x^k + Ã⁻¹·r,   r = b(x^k) − Ã·x^k,
 // which is the same map in exact arithmetic. r is small and smooth once the iteration is under
 // way, so an FP32 inverse and FP32 arithmetic for r leave an error of about 2⁻²⁴·|x^{k+1} − x^k|
-// per iteration instead of 2⁻²⁴·|x|, while positions stay FP64 and the fixed point is exactly
-// the reference's (r = 0). r needs no matrix: with the projections d_e at x^k,
-//   r_v = m_v/h²·(x̂_v − x_v) − Σ_e ±κ_e·(x_a − x_b − d_e) + Σ_s (−k_s w_v)·(w_sᵀx)  (free v),
+// per iteration instead of 2⁻²⁴·|x|, while positions keep ≈48-bit significands and the fixed
+// point is the reference's (r = 0). r needs no matrix: with the projections d_e at x^k,
+//   r_v = m_v/h²·(x̂_v − x_v) − Σ_e κ_e·((x_v − x_o) − d_e) + Σ_s (−k_s w_v)·(w_sᵀx)  (free v),
 // the mass, edge and bend terms of Ã (Assembler.cpp:139-278) with pinned neighbours at q, and
 // r_v = 0 with x_v = q_v for pinned rows. The same pass gives the reference's residual t_v
 // (Integrator.cpp:230-263) of x^k for the convergence gate.
 //
 // GB300 layout: one cloth is run by `team` CTAs (up to one per SM), each owning a contiguous
-// range of vertices and the matching rows of Ã⁻¹, kept in its shared memory when they fit. Per
-// iteration a CTA computes r for its vertices (FP32, positions as FP32 hi/lo pairs so that
-// differences keep FP64 accuracy), publishes them to L2, meets the team at a barrier, reads the
-// whole r, applies its rows of Ã⁻¹ (FP32 FMA from shared memory), updates its positions in FP64,
-// publishes them and meets the team again. FP64 instructions — 1/69 of the FP32 rate on this
-// part — are left only for the per-vertex position updates. The team barrier is an arrival
-// counter in global memory polled with acquire loads; the launch is cooperative so that every CTA
-// of the team is resident, and every wait gives up after a bounded number of polls, setting the
+// range of vertices, their incidences (in shared memory) and the matching rows of Ã⁻¹ (in shared
+// memory when they fit). Per iteration a CTA computes r for its vertices in FP32 (positions as
+// FP32 hi/lo pairs, so that differences keep FP64 accuracy) and publishes it; after exchange A it
+// holds the whole r, applies its rows of Ã⁻¹ (FP32 FMA from shared memory), updates its positions
+// and publishes them; after exchange B it holds the positions its vertices touch. Positions live
+// as FP32 hi/lo pairs (≈48-bit significands) updated with an exact two-sum, so the iteration loop
+// has no FP64 instruction — FP64 runs at 1/69 of the FP32 rate on this part; FP64 is left for the
+// once-per-substep prediction and velocity update.
+//
+// Exchanges go through L2 as 64-bit words (epoch << 32 | FP32 bits) written and read with
+// relaxed gpu-scope accesses: a reader polls the words it needs until each carries the current
+// epoch, so an exchange costs about one L2 round trip after the last writer and needs no fence
+// (a fence would also drop the L1 lines the CTA reads through). Per-CTA partial maxima (residual,
+// displacement, scale) travel the same way, one per L2 line; one warp polls them first and the
+// data words are read once every CTA has published, which keeps waiting CTAs from flooding L2. A word is rewritten only two exchanges later, which
+// no CTA reaches before every CTA has read it. The launch is cooperative so that every CTA of the
+// team is resident, and every poll gives up after a bounded number of rounds, setting the
 // instance's error flag.
 #include <cstdint>
 
@@ -30,52 +39,99 @@ namespace pdg {
 namespace {
 
 constexpr int kWarps = kDeltaThreads / 32;
-constexpr int kGroup = 16;                 // lanes per vertex in the correction pass
-constexpr long long kSpinLimit = 1ll << 22; // polls of the team counter before giving up
+constexpr int kGroup = 16;                  // lanes per vertex in the correction pass
+constexpr long long kSpinLimit = 1ll << 22; // poll rounds before an exchange gives up
+constexpr int kMaxTeam = 256;               // partials one polling warp covers (kMaxTeam / 32 a lane)
+constexpr int kSegments = 4;                // most column segments a row pair of Ã⁻¹ is split into
+constexpr int kPartStride = 16;             // words between two CTAs' partials: one L2 line each
 
-__device__ __forceinline__ unsigned long long loadAcquire(const unsigned long long* p) {
+__device__ __forceinline__ unsigned long long loadRelaxed(const unsigned long long* p) {
   unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 
-// Barrier of the team's CTAs. `publish` runs in thread 0 after the CTA's own threads have met and
-// before the arrival is released. Returns false in every thread when the wait gave up.
-template <class Publish>
-__device__ __forceinline__ bool teamBarrier(const InstanceDev& I, int team, unsigned long long& target,
-                                            volatile int* flag, Publish&& publish) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    publish();
-    target += static_cast<unsigned long long>(team);
-    __threadfence();
-    atomicAdd(I.bar, 1ull);
-    int ok = 1;
+__device__ __forceinline__ void storeRelaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long tagged(unsigned tag, float v) {
+  return (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
+}
+
+// Polls src[j] for j in [b, e) until each carries `tag` and hands its value to sink(j, value);
+// thread `tid` of `nth` takes every nth word, B loads in flight. False if a word stayed stale for
+// kSpinLimit rounds.
+template <int B, class Sink>
+__device__ __forceinline__ bool pollWords(const unsigned long long* src, int b, int e, unsigned tag, int tid, int nth,
+                                          Sink&& sink) {
+  for (int j0 = b + tid; j0 < e; j0 += B * nth) {
+    unsigned pending = 0;
+#pragma unroll
+    for (int u = 0; u < B; ++u)
+      if (j0 + u * nth < e) pending |= 1u << u;
     long long spins = 0;
-    while (loadAcquire(I.bar) < target) {
-      if (++spins > kSpinLimit) {
-        ok = 0;
-        atomicExch(I.err, 1);
-        break;
+    while (pending) {
+      unsigned long long w[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) w[u] = ((pending >> u) & 1u) ? loadRelaxed(src + j0 + u * nth) : 0ull;
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        if (((pending >> u) & 1u) && static_cast<unsigned>(w[u] >> 32) == tag) {
+          sink(j0 + u * nth, __uint_as_float(static_cast<unsigned>(w[u])));
+          pending &= ~(1u << u);
+        }
+      }
+      if (pending && ++spins > kSpinLimit) return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ float warpMaxF(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Warp 0: maximum of the team's partials tagged `tag` into *out (other warps return true).
+__device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int team, unsigned tag, float* out) {
+  if (threadIdx.x >= 32) return true;
+  const int lane = threadIdx.x;
+  unsigned pending = 0;
+#pragma unroll
+  for (int i = 0; i < kMaxTeam / 32; ++i)
+    if (lane + 32 * i < team) pending |= 1u << i;
+  float mx = 0.f;
+  long long spins = 0;
+  bool good = true;
+  while (true) {
+    unsigned long long w[kMaxTeam / 32];
+#pragma unroll
+    for (int i = 0; i < kMaxTeam / 32; ++i)
+      w[i] = ((pending >> i) & 1u) ? loadRelaxed(ptag + kPartStride * (lane + 32 * i)) : 0ull;
+#pragma unroll
+    for (int i = 0; i < kMaxTeam / 32; ++i) {
+      if (((pending >> i) & 1u) && static_cast<unsigned>(w[i] >> 32) == tag) {
+        mx = fmaxf(mx, __uint_as_float(static_cast<unsigned>(w[i])));
+        pending &= ~(1u << i);
       }
     }
-    __threadfence();
-    *flag = ok;
+    if (__all_sync(0xffffffffu, pending == 0)) break;
+    if (++spins > kSpinLimit) {
+      good = false;
+      break;
+    }
   }
-  __syncthreads();
-  return *flag != 0;
+  mx = warpMaxF(mx);
+  if (lane == 0) *out = mx;
+  return good;
 }
 
 template <int G>
 __device__ __forceinline__ float groupSum(float v) {
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-__device__ __forceinline__ float warpMaxF(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -96,18 +152,27 @@ __device__ __forceinline__ float3 diffHL(float4 ah, float4 al, float4 bh, float4
   return make_float3((ah.x - bh.x) + (al.x - bl.x), (ah.y - bh.y) + (al.y - bl.y), (ah.z - bh.z) + (al.z - bl.z));
 }
 
+// Pin position q_u as the hi/lo pair the host split it into.
 __device__ __forceinline__ void pinHL(const InstanceDev& I, int u, float4& h, float4& l) {
-  split(I.q[3 * u], h.x, l.x);
-  split(I.q[3 * u + 1], h.y, l.y);
-  split(I.q[3 * u + 2], h.z, l.z);
-  h.w = l.w = 0.f;
+  h = __ldg(I.qhl + 2 * u);
+  l = __ldg(I.qhl + 2 * u + 1);
 }
 
-// Rows of Ã⁻¹ times the three components of R, two rows per warp; A rows from shared or global
-// memory. Sums of the pair land in dl[3·li + c].
+// (hi, lo) + d as a renormalised pair: Knuth's two-sum of hi and d, then a fast two-sum.
+__device__ __forceinline__ void addHL(float& hi, float& lo, float d) {
+  const float s = hi + d;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (d - bb);
+  const float l = lo + e;
+  hi = s + l;
+  lo = l - (hi - s);
+}
+
+// Rows of Ã⁻¹ times the three components of R over the float4 columns [jb, je), two rows per
+// warp; A rows from shared or global memory. Sums of the pair land in dl[3·li + c].
 template <bool SMEM>
 __device__ __forceinline__ void rowPair(const float* A0, const float* A1, bool two, const float* Rs, int ld, int li,
-                                        float* dl) {
+                                        int jb, int je, float* dl) {
   const int lane = threadIdx.x & 31;
   const float4* a0 = reinterpret_cast<const float4*>(A0);
   const float4* a1 = reinterpret_cast<const float4*>(A1);
@@ -115,9 +180,8 @@ __device__ __forceinline__ void rowPair(const float* A0, const float* A1, bool t
   const float4* ry = reinterpret_cast<const float4*>(Rs + ld);
   const float4* rz = reinterpret_cast<const float4*>(Rs + 2 * ld);
   float s0 = 0.f, s1 = 0.f, s2 = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
-  const int q4 = ld / 4;
 #pragma unroll 4
-  for (int j = lane; j < q4; j += 32) {
+  for (int j = jb + lane; j < je; j += 32) {
     const float4 x = rx[j], y = ry[j], z = rz[j];
     const float4 u = SMEM ? a0[j] : __ldg(a0 + j);
     const float4 w = SMEM ? a1[j] : __ldg(a1 + j);
@@ -149,10 +213,9 @@ __device__ __forceinline__ void rowPair(const float* A0, const float* A1, bool t
 __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const InstanceDev* __restrict__ insts,
                                                                       int team, int substeps) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double redD[kWarps];
-  __shared__ float redF[kWarps];
-  __shared__ double gate[3];
-  __shared__ int flag;
+  __shared__ float red[kWarps];
+  __shared__ float gate;
+  __shared__ int failed;
   const int rank = static_cast<int>(blockIdx.x) % team;
   const InstanceDev& I = insts[blockIdx.x / team];
   const int n = I.n, ld = I.denseLd;
@@ -161,21 +224,34 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   const int resRows = min(m, I.denseResRows);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // shared memory: all positions (hi/lo), the whole correction, resident rows of Ã⁻¹, own FP64 state
+  // shared memory (16-byte items first): positions as hi/lo pairs, the whole correction, resident
+  // rows of Ã⁻¹, own incidences, vertex constants and x̂ (hi/lo), x_n and v (FP64), partial sums
+  // of Δ per column segment, incidence offsets
   float4* Xs = reinterpret_cast<float4*>(smem);
+  float* xf = reinterpret_cast<float*>(Xs);  // vertex v: hi at xf[8v + c], lo at xf[8v + 4 + c]
   float* Rs = reinterpret_cast<float*>(Xs + 2 * n);
   float* As = Rs + 3 * ld;
-  double* xo = reinterpret_cast<double*>(As + static_cast<size_t>(I.denseResRows) * ld);
-  double* xno = xo + 3 * chunk;
-  double* xho = xno + 3 * chunk;
-  double* vo = xho + 3 * chunk;
-  float* dl = reinterpret_cast<float*>(vo + 3 * chunk);
-  float4* xbuf4 = reinterpret_cast<float4*>(I.xbuf);
+  int4* sE = reinterpret_cast<int4*>(As + static_cast<size_t>(I.denseResRows) * ld);
+  int4* sB = sE + I.teamECap;
+  float4* sV = reinterpret_cast<float4*>(sB + I.teamBCap);
+  float4* sXh = sV + chunk;
+  double* xn64 = reinterpret_cast<double*>(sXh + 2 * chunk);
+  double* v64 = xn64 + 3 * chunk;
+  float* dl = reinterpret_cast<float*>(v64 + 3 * chunk);  // kSegments × 3·chunk
+  int* sEb = reinterpret_cast<int*>(dl + kSegments * 3 * chunk);
+  int* sBb = sEb + chunk + 1;
 
-  for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
-    xo[t] = I.x[3 * rb + t];
-    vo[t] = I.v[3 * rb + t];
+  if (threadIdx.x == 0) failed = 0;
+  const int e0 = (m > 0) ? I.rstart[rb] : 0, b0 = (m > 0) ? I.bstart[rb] : 0;
+  const int eN = (m > 0) ? I.rstart[re] - e0 : 0, bN = (m > 0) ? I.bstart[re] - b0 : 0;
+  for (int t = threadIdx.x; t < eN; t += blockDim.x) sE[t] = I.tEdge[e0 + t];
+  for (int t = threadIdx.x; t < bN; t += blockDim.x) sB[t] = I.tBend[b0 + t];
+  for (int t = threadIdx.x; t < m; t += blockDim.x) sV[t] = I.tVtx[rb + t];
+  for (int t = threadIdx.x; t <= m; t += blockDim.x) {
+    sEb[t] = I.rstart[rb + t] - e0;
+    sBb[t] = I.bstart[rb + t] - b0;
   }
+  for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) v64[t] = I.v[3 * rb + t];
   for (int v = threadIdx.x; v < n; v += blockDim.x) {
     float4 h, l;
     split(I.x[3 * v], h.x, l.x);
@@ -192,50 +268,57 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     const int total = resRows * (ld / 4);
     for (int t = threadIdx.x; t < total; t += blockDim.x) dst[t] = __ldg(src + t);
   }
-  // barrier arrivals so far: a multiple of `team` (no CTA can pass the first barrier before this
-  // CTA arrives there, so at most team − 1 arrivals of this launch can have been counted)
-  unsigned long long target = 0;
-  if (threadIdx.x == 0) target = loadAcquire(I.bar) / team * team;
-  int parity = 0;
+  unsigned epoch = *I.epoch;  // exchanges of this launch continue the previous launch's epochs
+  unsigned long long* ptagA = I.ptag;
+  unsigned long long* ptagB = I.ptag + kPartStride * team;
+  const int wlo = I.window[2 * rank], whi = I.window[2 * rank + 1];
+  // GEMV work: row pairs × column segments over the warps
+  const int pairs = (m + 1) / 2;
+  const int segs = pairs > 0 ? max(1, min(kSegments, kWarps / pairs)) : 1;
+  const int q4 = ld / 4;
   __syncthreads();
 
   for (int step = 0; step < substeps; ++step) {
-    // predict own rows (Integrator.cpp:447-472)
+    // predict own rows (Integrator.cpp:447-472), x̂ kept as a hi/lo pair
     double sc = 0.0;
     for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
-      const int c = t % 3;
-      const double p = xo[t];
-      const double xh = (p + vo[t] * I.h) + I.gh2[c];
-      xno[t] = p;
-      xho[t] = xh;
+      const int li = t / 3, c = t - 3 * li, v = rb + li;
+      const double p = static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+      const double xh = (p + v64[t] * I.h) + I.gh2[c];
+      xn64[t] = p;
+      float hi, lo;
+      split(xh, hi, lo);
+      float* xhf = reinterpret_cast<float*>(sXh);
+      xhf[8 * li + c] = hi;
+      xhf[8 * li + 4 + c] = lo;
       sc = fmax(sc, fabs(xh - p));
     }
-    sc = warpMaxD(sc);
-    if (lane == 0) redD[warp] = sc;
+    const float scW = static_cast<float>(warpMaxD(sc));
     __syncthreads();  // x̂ of own rows is read by other threads below
     double scale = 0.0;
     int used = 0;
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
     for (int k = 0;; ++k) {
-      // correction r and residual of x^k for own vertices, kGroup lanes per vertex
+      const unsigned tagA = ++epoch;
+      // correction r and residual of x^k for own vertices, kGroup lanes per vertex (FP32 only)
       float resLocal = 0.f;
       const int gl = threadIdx.x & (kGroup - 1), group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
       for (int base = 0; base < m; base += ngroups) {
         const int li = base + group;
         const bool active = li < m;
-        const int v = rb + (active ? li : 0);
+        const float4 vc = active ? sV[li] : make_float4(0.f, 0.f, 1.f, 0.f);
+        const int v = rb + li;
         // a: mass + edge terms of the residual, f: its bend terms, p: what the matrix adds to
-        // −(a) + f because it couples pinned neighbours at q rather than at their positions
+        // f − a because it couples pinned neighbours at q rather than at their positions
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f, p0 = 0.f, p1 = 0.f, p2 = 0.f;
-        if (active && !I.pinned[v]) {
-          for (int q = I.rstart[v] + gl; q < I.rstart[v + 1]; q += kGroup) {
-            const int p = I.rinc[q];
-            const int e = p >> 1;
-            const int a = I.eab[2 * e], b = I.eab[2 * e + 1];
-            const float4 ah = Xs[2 * a], al = Xs[2 * a + 1], bh = Xs[2 * b], bl = Xs[2 * b + 1];
-            const float3 rel = diffHL(ah, al, bh, bl);
-            const float rest = __ldg(I.edge32 + 2 * e), kap = __ldg(I.edge32 + 2 * e + 1);
+        if (vc.z == 0.f) {
+          const float4 vh = Xs[2 * v], vl = Xs[2 * v + 1];
+          for (int q = sEb[li] + gl; q < sEb[li + 1]; q += kGroup) {
+            const int4 E = sE[q];
+            const int o = E.x & 0x7fffffff;
+            const float rest = __int_as_float(E.y), kap = __int_as_float(E.z);
+            const float3 rel = diffHL(vh, vl, Xs[2 * o], Xs[2 * o + 1]);  // x_v − x_o
             const float len = sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
             float dx = 0.f, dy = 0.f, dz = 0.f;
             if (!(len <= 1e-12f)) {
@@ -244,42 +327,44 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
               dy = rel.y * s;
               dz = rel.z * s;
             }
-            const float sg = (p & 1) ? -1.f : 1.f;
-            // residual: rc_e = κ·(x_a − x_b) − κ·d_e at the current positions
-            a0 = fmaf(sg * kap, rel.x - dx, a0);
-            a1 = fmaf(sg * kap, rel.y - dy, a1);
-            a2 = fmaf(sg * kap, rel.z - dz, a2);
-            // the matrix couples a free vertex to a pinned neighbour at q, not at its position
-            const int other = (p & 1) ? a : b;
-            if (I.pinned[other]) {
+            // ±rc_e = κ·(x_a − x_b) − κ·d_e seen from v (the projection is odd in x_a − x_b)
+            a0 = fmaf(kap, rel.x - dx, a0);
+            a1 = fmaf(kap, rel.y - dy, a1);
+            a2 = fmaf(kap, rel.z - dz, a2);
+            if (E.x < 0) {  // pinned neighbour: the matrix sees it at q
               float4 qh, ql;
-              pinHL(I, other, qh, ql);
-              const float3 relq = (p & 1) ? diffHL(qh, ql, bh, bl) : diffHL(ah, al, qh, ql);
-              p0 = fmaf(sg * kap, relq.x - rel.x, p0);
-              p1 = fmaf(sg * kap, relq.y - rel.y, p1);
-              p2 = fmaf(sg * kap, relq.z - rel.z, p2);
+              pinHL(I, o, qh, ql);
+              const float3 relq = diffHL(vh, vl, qh, ql);
+              p0 = fmaf(kap, relq.x - rel.x, p0);
+              p1 = fmaf(kap, relq.y - rel.y, p1);
+              p2 = fmaf(kap, relq.z - rel.z, p2);
             }
           }
-          for (int q = I.bstart[v] + gl; q < I.bstart[v + 1]; q += kGroup) {
-            const int s = I.binc[q];
-            const int a = I.babc[3 * s], b = I.babc[3 * s + 1], c = I.babc[3 * s + 2];
-            const float fac = __ldg(I.bfac32 + q);
+          for (int q = sBb[li] + gl; q < sBb[li + 1]; q += kGroup) {
+            const int4 S = sB[q];
+            const int a = S.x & 0x7fffffff, b = S.y & 0x7fffffff, c = S.z & 0x7fffffff;
+            const float fac = __int_as_float(S.w);
             float4 ah = Xs[2 * a], al = Xs[2 * a + 1], bh = Xs[2 * b], bl = Xs[2 * b + 1], ch = Xs[2 * c],
                    cl = Xs[2 * c + 1];
             const float3 u = diffHL(ah, al, bh, bl), w = diffHL(ch, cl, bh, bl);
             f0 = fmaf(fac, u.x + w.x, f0);
             f1 = fmaf(fac, u.y + w.y, f1);
             f2 = fmaf(fac, u.z + w.z, f2);
-            const bool pa = I.pinned[a], pb = I.pinned[b], pc = I.pinned[c];
-            if (pa || pb || pc) {  // matrix part with pinned members at q
-              if (pa) pinHL(I, a, ah, al);
-              if (pb) pinHL(I, b, bh, bl);
-              if (pc) pinHL(I, c, ch, cl);
+            if ((S.x | S.y | S.z) < 0) {  // pinned members: the matrix part sees them at q
+              if (S.x < 0) pinHL(I, a, ah, al);
+              if (S.y < 0) pinHL(I, b, bh, bl);
+              if (S.z < 0) pinHL(I, c, ch, cl);
               const float3 uq = diffHL(ah, al, bh, bl), wq = diffHL(ch, cl, bh, bl);
               p0 = fmaf(fac, (u.x + w.x) - (uq.x + wq.x), p0);
               p1 = fmaf(fac, (u.y + w.y) - (uq.y + wq.y), p1);
               p2 = fmaf(fac, (u.z + w.z) - (uq.z + wq.z), p2);
             }
+          }
+          if (gl == 0) {  // mass term (x − x̂)·m/h²
+            const float3 dx = diffHL(vh, vl, sXh[2 * li], sXh[2 * li + 1]);
+            a0 = fmaf(dx.x, vc.x, a0);
+            a1 = fmaf(dx.y, vc.x, a1);
+            a2 = fmaf(dx.z, vc.x, a2);
           }
         }
         a0 = groupSum<kGroup>(a0);
@@ -293,14 +378,10 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         p2 = groupSum<kGroup>(p2);
         if (active && gl == 0) {
           float r0 = 0.f, r1 = 0.f, r2 = 0.f;
-          if (!I.pinned[v]) {
-            const float mh2 = __ldg(I.vtx32 + 2 * v), invM = __ldg(I.vtx32 + 2 * v + 1);
-            a0 = fmaf(static_cast<float>(xo[3 * li] - xho[3 * li]), mh2, a0);
-            a1 = fmaf(static_cast<float>(xo[3 * li + 1] - xho[3 * li + 1]), mh2, a1);
-            a2 = fmaf(static_cast<float>(xo[3 * li + 2] - xho[3 * li + 2]), mh2, a2);
-            if (invM > 0.f) {
+          if (vc.z == 0.f) {
+            if (vc.y > 0.f) {
               const float t0 = a0 + f0, t1 = a1 + f1, t2 = a2 + f2;
-              resLocal = fmaxf(resLocal, sqrtf(t0 * t0 + t1 * t1 + t2 * t2) * invM);
+              resLocal = fmaxf(resLocal, sqrtf(t0 * t0 + t1 * t1 + t2 * t2) * vc.y);
             }
             // r = −(mass + edge terms) + bend terms with pinned neighbours at q (the pinned part
             // of the bend terms is the reference's constant bending RHS)
@@ -308,101 +389,108 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
             r1 = (f1 - a1) - p1;
             r2 = (f2 - a2) - p2;
           }
-          I.rbuf[v] = r0;
-          I.rbuf[ld + v] = r1;
-          I.rbuf[2 * ld + v] = r2;
+          storeRelaxed(I.rtag + v, tagged(tagA, r0));
+          storeRelaxed(I.rtag + n + v, tagged(tagA, r1));
+          storeRelaxed(I.rtag + 2 * n + v, tagged(tagA, r2));
         }
       }
+      // exchange A: the whole correction (warps 1..), the maximum of the residuals — at k = 0 of
+      // the scale — (warp 0)
       resLocal = warpMaxF(resLocal);
-      if (lane == 0) redF[warp] = resLocal;
-      // barrier A: the correction is complete; partial maxima of the residual (and at k = 0 the scale)
-      double* slotA = I.part + 3 * (parity * team + rank);
-      if (!teamBarrier(I, team, target, &flag, [&] {
-            double rm = 0.0, sm = 0.0;
-            for (int w = 0; w < kWarps; ++w) {
-              rm = fmax(rm, static_cast<double>(redF[w]));
-              sm = fmax(sm, redD[w]);
-            }
-            slotA[0] = rm;
-            slotA[2] = sm;
-          }))
-        return;
-      if (warp == 0) {
-        double rm = 0.0, sm = 0.0;
-        for (int r = lane; r < team; r += 32) {
-          rm = fmax(rm, __ldcg(I.part + 3 * (parity * team + r)));
-          sm = fmax(sm, __ldcg(I.part + 3 * (parity * team + r) + 2));
-        }
-        rm = warpMaxD(rm);
-        sm = warpMaxD(sm);
-        if (lane == 0) {
-          gate[0] = rm;
-          gate[2] = sm;
-        }
-      }
+      if (lane == 0) red[warp] = (k == 0) ? scW : resLocal;
       __syncthreads();
-      parity ^= 1;
-      if (k == 0) scale = (gate[2] < I.gScaleHH) ? I.gScaleHH : gate[2];
+      bool ok = true;
+      if (warp == 0) {
+        if (lane == 0) {
+          float pm = 0.f;
+          for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
+          storeRelaxed(ptagA + kPartStride * rank, tagged(tagA, pm));
+        }
+        __syncwarp();
+        ok = pollPartials(ptagA, team, tagA, &gate);
+      }
+      if (!ok) failed = 1;
+      __syncthreads();  // every CTA has published: the words below are (almost always) current
+      if (failed) break;
+      ok = pollWords<10>(I.rtag, 0, 3 * n, tagA, threadIdx.x, blockDim.x, [&](int j, float val) {
+        const int c = j / n;
+        Rs[c * ld + (j - c * n)] = val;
+      });
+      if (!ok) failed = 1;
+      __syncthreads();
+      if (failed) break;
+      const double gateA = gate;
+      if (k == 0) scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
       if (I.useResidual && k >= 1) {
-        lastRes = gate[0];
+        lastRes = gateA;
         used = k;
-        conv = gate[0] <= I.resThreshold;
+        conv = gateA <= I.resThreshold;
         if (conv) break;
       }
       if (k == I.maxIter) break;
 
-      // whole correction into shared memory, then this CTA's rows of Ã⁻¹·r
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        Rs[j] = __ldcg(I.rbuf + j);
-        Rs[ld + j] = __ldcg(I.rbuf + ld + j);
-        Rs[2 * ld + j] = __ldcg(I.rbuf + 2 * ld + j);
-      }
-      __syncthreads();
-      for (int li = 2 * warp; li < m; li += 2 * kWarps) {
+      // this CTA's rows of Ã⁻¹·r: row pairs × column segments over the warps
+      for (int task = warp; task < pairs * segs; task += kWarps) {
+        const int li = 2 * (task / segs), sg = task - (task / segs) * segs;
+        const int jb = q4 * sg / segs, je = q4 * (sg + 1) / segs;
         const bool two = li + 1 < m;
-        if (li < resRows) {  // resRows is even: both rows of the pair are resident
+        float* out = dl + sg * 3 * chunk;
+        if (li < resRows) {  // resRows is even unless it covers every row: the pair is resident
           const float* A0 = As + static_cast<size_t>(li) * ld;
-          rowPair<true>(A0, two ? A0 + ld : A0, two, Rs, ld, li, dl);
+          rowPair<true>(A0, two ? A0 + ld : A0, two, Rs, ld, li, jb, je, out);
         } else {
           const float* A0 = I.Ainv + static_cast<size_t>(rb + li) * ld;
-          rowPair<false>(A0, two ? A0 + ld : A0, two, Rs, ld, li, dl);
+          rowPair<false>(A0, two ? A0 + ld : A0, two, Rs, ld, li, jb, je, out);
         }
       }
       __syncthreads();
-      // x^{k+1} = x^k + Δ in FP64 (pinned rows: q), published as hi/lo pairs
-      double dmax = 0.0;
-      float* xb = I.xbuf;
+      // x^{k+1} = x^k + Δ as hi/lo pairs (pinned rows: q), published for the team
+      const unsigned tagB = ++epoch;
+      float dmax = 0.f;
       for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
         const int li = t / 3, c = t - 3 * li, v = rb + li;
-        const double xn = I.pinned[v] ? I.q[3 * v + c] : xo[t] + static_cast<double>(dl[t]);
-        dmax = fmax(dmax, fabs(xn - xo[t]));
-        xo[t] = xn;
-        float hi, lo;
-        split(xn, hi, lo);
-        __stcg(xb + 8 * v + c, hi);
-        __stcg(xb + 8 * v + 4 + c, lo);
+        float hi = xf[8 * v + c], lo = xf[8 * v + 4 + c];
+        if (sV[li].z != 0.f) {
+          const float* qf = reinterpret_cast<const float*>(I.qhl);
+          const float qh = __ldg(qf + 8 * v + c), ql = __ldg(qf + 8 * v + 4 + c);
+          dmax = fmaxf(dmax, fabsf((qh - hi) + (ql - lo)));
+          hi = qh;
+          lo = ql;
+        } else {
+          float d = dl[t];
+          for (int sgi = 1; sgi < segs; ++sgi) d += dl[sgi * 3 * chunk + t];
+          dmax = fmaxf(dmax, fabsf(d));
+          addHL(hi, lo, d);
+        }
+        storeRelaxed(I.xtag + 6 * v + c, tagged(tagB, hi));
+        storeRelaxed(I.xtag + 6 * v + 3 + c, tagged(tagB, lo));
       }
-      dmax = warpMaxD(dmax);
-      if (lane == 0) redD[warp] = dmax;
-      // barrier B: new positions complete; partial maxima of the displacement
-      double* slotB = I.part + 3 * (parity * team + rank);
-      if (!teamBarrier(I, team, target, &flag, [&] {
-            double dm = 0.0;
-            for (int w = 0; w < kWarps; ++w) dm = fmax(dm, redD[w]);
-            slotB[1] = dm;
-          }))
-        return;
-      for (int j = threadIdx.x; j < 2 * n; j += blockDim.x) Xs[j] = __ldcg(xbuf4 + j);
-      if (warp == 0) {
-        double dm = 0.0;
-        for (int r = lane; r < team; r += 32) dm = fmax(dm, __ldcg(I.part + 3 * (parity * team + r) + 1));
-        dm = warpMaxD(dm);
-        if (lane == 0) gate[1] = dm;
-      }
+      // exchange B: the positions this CTA reads (warps 1..), the maximum of the displacements
+      // (warp 0)
+      dmax = warpMaxF(dmax);
+      if (lane == 0) red[warp] = dmax;
       __syncthreads();
-      parity ^= 1;
+      if (warp == 0) {
+        if (lane == 0) {
+          float pm = 0.f;
+          for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
+          storeRelaxed(ptagB + kPartStride * rank, tagged(tagB, pm));
+        }
+        __syncwarp();
+        ok = pollPartials(ptagB, team, tagB, &gate);
+      }
+      if (!ok) failed = 1;
+      __syncthreads();
+      if (failed) break;
+      ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x, blockDim.x, [&](int j, float val) {
+        const int v = j / 6, c = j - 6 * v;  // c < 3: hi, else lo
+        xf[8 * v + (c < 3 ? c : c + 1)] = val;
+      });
+      if (!ok) failed = 1;
+      __syncthreads();
+      if (failed) break;
       if (!I.useResidual) {
-        const double diff = gate[1];
+        const double diff = gate;
         const double rel = (scale > 0.0) ? diff / scale : diff;
         const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
         const bool relHit = (I.relTol > 0.0) && (rel <= I.relTol);
@@ -411,14 +499,18 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         if (conv) break;
       }
     }
+    if (failed) {
+      if (threadIdx.x == 0) atomicExch(I.err, 1);
+      return;
+    }
     // velocity, damping, pin resnap (Integrator.cpp:774-791)
     for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
-      const int v = rb + t / 3;
-      if (I.pinned[v]) {
-        xo[t] = I.q[3 * rb + t];
-        vo[t] = 0.0;
+      const int li = t / 3, c = t - 3 * li, v = rb + li;
+      if (sV[li].z != 0.f) {
+        v64[t] = 0.0;
       } else {
-        vo[t] = (xo[t] - xno[t]) * I.dampInvH;
+        const double x = static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+        v64[t] = (x - xn64[t]) * I.dampInvH;
       }
     }
     if (used == 0) {  // no update ran: pinned vertices are resnapped to q everywhere
@@ -435,11 +527,13 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     }
     __syncthreads();
   }
+  if (rank == 0 && threadIdx.x == 0) *I.epoch = epoch;
   for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
-    I.x[3 * rb + t] = xo[t];
-    I.v[3 * rb + t] = vo[t];
-    I.xn[3 * rb + t] = xno[t];
-    I.xhat[3 * rb + t] = xho[t];
+    const int li = t / 3, c = t - 3 * li, v = rb + li;
+    I.x[3 * rb + t] = (sV[li].z != 0.f) ? I.q[3 * v + c]
+                                         : static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+    I.v[3 * rb + t] = v64[t];
+    I.xn[3 * rb + t] = xn64[t];
   }
 }
 
@@ -462,7 +556,8 @@ int deltaResidentCtas(int smemBytes) {
 
 int launchSubstepDelta(const InstanceDev* d, int count, int team, int smemBytes, int substeps, void* stream) {
   if (count <= 0 || substeps <= 0) return 0;
-  if (deltaResidentCtas(smemBytes) < count * team) return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
+  if (team > kMaxTeam || deltaResidentCtas(smemBytes) < count * team)
+    return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(count * team);
   cfg.blockDim = dim3(kDeltaThreads);
