@@ -2,16 +2,19 @@
 
 A step is one PD substep (predict, K iterations, velocity update) of the workload's cloth(s).
 Default workload: the 40×40 cloth with distance, shear and bend constraints, 40 iterations and
-a 1e-3·|g| residual gate (``pd_gb300.workloads.cloth40_full``).
+a 1e-3·|g| residual gate (``pd_gb300.workloads.cloth40_full``), in the MIXED precision mode.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--precision MODE]
+                  [--impl ours|reference]
 
 Prints one JSON line. ``value`` times the substep kernel with its data resident in HBM (CUDA
 events on the simulator's stream, L2 flushed between timed steps); ``e2e`` times the same
 substeps through the C ABI with the state copied from pinned host memory and read back every
-step. ``--impl reference`` times the CPU oracle (the reference algorithm restated) on all host
-cores instead. Under torchrun each rank steps its own cloth(s) (replicas; no collective on the
-data path) and rank 0 reports the aggregate.
+step. Beside them: ``pos_err`` (the mode's position error against the FP64 CPU oracle after the
+workload's full substep count), ``fp64_gpu`` (the plain one-cloth-per-launch FP64 GPU path on the
+same workload) and ``cpu_baseline``. ``--impl reference`` times the CPU oracle (the reference
+algorithm restated) on all host cores instead. Under torchrun each rank steps its own cloth(s)
+(replicas; no collective on the data path) and rank 0 reports the aggregate.
 """
 from __future__ import annotations
 
@@ -29,8 +32,25 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "PD substeps/s (1 cloth & 512-batch) vs plain FP64 GPU at 1e-5 pos err; grads/s"
-# precision modes of the GPU substep: name -> (PD_PRECISION_* value, dtype label, kernel name)
-PRECISIONS = {"fp64-exact": (0, "f64", "substepExactKernel"), "fp64": (1, "f64", "substepFastKernel")}
+# precision modes of the GPU substep: name -> (PD_PRECISION_* value, arithmetic label)
+PRECISIONS = {"fp64-exact": (0, "f64"), "fp64": (1, "f64"), "fp32-projection": (2, "f64 (f32 projection)"),
+              "fp32-solve": (3, "f64 (f32 solve + f64 refinement)"),
+              "mixed": (4, "f32 (positions as f32 hi/lo pairs)")}
+POS_ERR_BOUND = 1e-5
+
+
+def kernel_name(info):
+    """The substep kernel a simulator launches, from its solve kind and CTAs per cloth."""
+    kind, ctas = info["solve_kind"], info["cluster_ctas"]
+    if kind == 0:
+        return "substepExactKernel"
+    if kind == 1:
+        return "substepClusterKernel" if ctas > 1 else "substepFastKernel"
+    if kind == 2:
+        return "substepMixedClusterKernel" if ctas > 1 else "substepMixedKernel"
+    if kind == 3:
+        return "substepDenseClusterKernel"
+    return "substepDeltaKernel"
 UNIT = "substeps/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -38,14 +58,16 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=600)  # the workload's substep count, ≥ 0.2 s of clocks
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--workload", default="cloth40_full")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
+    p.add_argument("--precision", default="mixed", choices=list(PRECISIONS))
     p.add_argument("--batch-count", type=int, default=512)
     p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-pos-err", action="store_true")
+    p.add_argument("--no-fp64-gpu", action="store_true")
     return p.parse_args()
 
 
@@ -56,7 +78,7 @@ def dist_env():
     return rank, world, local
 
 
-def workload(name, batch_count, precision="fp64"):
+def workload(name, batch_count, precision="mixed"):
     import copy
     from pd_gb300 import workloads as W
     if name == "batch":
@@ -70,7 +92,7 @@ def workload(name, batch_count, precision="fp64"):
     return scenes, cfgs, sub
 
 
-def describe_workload(name, scenes, cfgs, precision="fp64"):
+def describe_workload(name, scenes, cfgs, precision="mixed"):
     c = cfgs[0]
     n = sum(s.n for s in scenes)
     e = sum(int(s.edges.shape[0]) for s in scenes)
@@ -81,14 +103,18 @@ def describe_workload(name, scenes, cfgs, precision="fp64"):
 
 
 # --------------------------------------------------------------------------------- roofline
-def algorithmic_bytes(scene, factor_nnz, iterations):
-    """Bytes one substep must move (the per-unit formula stated in the design doc)."""
+def algorithmic_bytes(scene, factor_nnz, iterations, precision="fp64"):
+    """Bytes one substep must move (the per-substep formula stated in the design doc): projection and
+    scatter, the two triangular solves over the factor's F entries, the residual, prediction and
+    velocity update. FP32 projection reads 12-byte positions; an FP32 solve reads 4-byte values."""
     n = scene.n
     E = int(scene.edges.shape[0])
     S = int(np.asarray(scene.bends).reshape(-1, 3).shape[0])
     F = factor_nnz
-    b_ps = 24 * n * 3 + (24 * n if S else 0) + 24 * E + 8 * E + 4 * (n + 1) + n
-    b_solve = 2 * F * (8 + 4) + 8 * n + 8 * (n + 1) + 2 * 24 * n + 8 * n
+    xb = 12 if precision in ("fp32-projection", "mixed") else 24
+    vb = 4 if precision in ("fp32-solve", "mixed") else 8
+    b_ps = xb * n + 24 * n * 2 + (24 * n if S else 0) + 24 * E + 8 * E + 4 * (n + 1) + n
+    b_solve = 2 * F * (vb + 4) + vb * n + 8 * (n + 1) + 2 * 24 * n + 8 * n
     b_res = 24 * n * 5 + 8 * n + 32 * E + 4 * (n + 1) + ((3 * S * 12 + 24 * S) if S else 0)
     return iterations * (b_ps + b_solve + b_res) + 96 * n + 72 * n
 
@@ -104,6 +130,28 @@ def fp64_ops(scene, factor_nnz, iterations):
     solve = 3 * (2 * F * 2 + n)                     # mul + sub per factor entry, both sweeps
     res = 2 * E * 3 + 3 * S * 9 + n * 16           # residual sums, bend force, inertia + norm
     return iterations * (edge + gather + solve + res) + edge + n * 12
+
+
+def profiled_traffic(kernel, workload_name, precision):
+    """DRAM bytes per substep of `kernel` on this workload from a committed ncu summary: a line
+    'bench-traffic <kernel> <workload> <precision>: <bytes>' in profiles/*.md, else None."""
+    key = f"bench-traffic {kernel} {workload_name} {precision}:"
+    d = os.path.join(ROOT, "profiles")
+    try:
+        names = sorted(os.listdir(d))
+    except OSError:
+        return None
+    for nm in names:
+        if not nm.endswith(".md"):
+            continue
+        with open(os.path.join(d, nm)) as f:
+            for line in f:
+                if line.strip().startswith(key):
+                    try:
+                        return float(line.split(":", 1)[1].split()[0])
+                    except (ValueError, IndexError):
+                        return None
+    return None
 
 
 def read_peaks():
@@ -127,7 +175,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -212,6 +260,44 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------ ours
+def time_fp64_gpu(P, args, stream, flush, max_steps=10):
+    """Substeps/s of the plain FP64 GPU path (supernodal solve, one cloth per launch) on the
+    workload, timed like `value`: one launch per substep, L2 flushed between substeps."""
+    import torch
+    scenes, cfgs, _ = workload(args.workload, args.batch_count, "fp64")
+    sim = P.Simulator(scenes, cfgs)
+    sim.set_stream(stream.cuda_stream)
+    k = min(args.steps, max_steps)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sim.step(1, sync=False)
+            flush.fill_(1.0)
+        for j in range(k):
+            flush.fill_(float(j))
+            starts[j].record(stream)
+            sim.step(1, sync=False)
+            ends[j].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / k
+    return {"value": 1e3 / ms, "unit": UNIT, "steps": k, "kernel": kernel_name(sim.info(0)),
+            "ctas_per_cloth": sim.info(0)["cluster_ctas"]}
+
+
+def position_error(P, args, scenes, cfgs, substeps):
+    """max |x_gpu − x_oracle| / max |x_oracle| of cloth 0 after `substeps` substeps from the
+    initial state, this precision mode against the FP64 CPU oracle."""
+    from tests.helpers import max_rel, oracle_twin  # checker only
+    sim = P.Simulator([scenes[0]], [cfgs[0]])
+    orc = oracle_twin(scenes[0], cfgs[0], perm=sim.factor(0)["perm"], threads=os.cpu_count())
+    sim.step(substeps)
+    orc.step(substeps)
+    err = max_rel(sim.state(0)[0], orc.state()[0])
+    return {"value": err, "bound": POS_ERR_BOUND, "within": bool(err <= POS_ERR_BOUND), "substeps": substeps,
+            "against": "FP64 CPU oracle (reference algorithm restated), cloth 0"}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -289,33 +375,49 @@ def run_ours(args):
         torch.distributed.all_reduce(e_local, op=torch.distributed.ReduceOp.MAX)
     e2e_value = world * args.steps / float(e_local.item())
 
+    # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
+    # error of this mode against the FP64 CPU oracle after the workload's full substep count
+    fp64_line = pos_err = None
+    if rank == 0:
+        if not args.no_fp64_gpu:
+            fp64_line = time_fp64_gpu(P, args, stream, flush)
+        if not args.no_pos_err:
+            pos_err = position_error(P, args, scenes, cfgs, sub)
+
     if rank == 0:
         info = sim.info(0)
-        iters = max(1, iters_used[0])
-        per_launch_bytes = sum(algorithmic_bytes(s, sim.info(i)["factor_nnz"], iters_used[i])
+        kernel = kernel_name(info)
+        per_launch_bytes = sum(algorithmic_bytes(s, sim.info(i)["factor_nnz"], iters_used[i], args.precision)
                                for i, s in enumerate(scenes))
-        ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
         peak, peak_kind = read_peaks()
         achieved = per_launch_bytes / (kernel_ms * 1e-3) / 1e9
-        fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU (profiles/)
-        fp64_achieved = ops / (kernel_ms * 1e-3) / 1e9
+        traffic = profiled_traffic(kernel, args.workload, args.precision)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": PRECISIONS[args.precision][1], "data": "synthetic",
                 "config": dict(describe_workload(args.workload, scenes, cfgs, args.precision),
                                l2="flushed between timed substeps (256 MB device write outside the timed events)",
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                               kernel=kernel, ctas_per_cloth=info["cluster_ctas"],
                                factor_nnz=info["factor_nnz"], iterations_used=iters_used[0]),
                 "wall_s": t_wall,
                 "gpu_launches": args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                             "kernel": PRECISIONS[args.precision][2],
-                             "algorithmic_bytes_per_launch": per_launch_bytes},
-                "fp64": {"achieved_gops": fp64_achieved, "peak_gops": fp64_peak,
-                         "frac": fp64_achieved / fp64_peak, "ops_per_launch": ops},
+                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                             "kernel": kernel, "algorithmic_bytes_per_launch": per_launch_bytes},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "clocks": clocks}
+        if PRECISIONS[args.precision][0] <= 1:
+            ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
+            fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU
+            fp64_achieved = ops / (kernel_ms * 1e-3) / 1e9
+            line["fp64"] = {"achieved_gops": fp64_achieved, "peak_gops": fp64_peak,
+                            "frac": fp64_achieved / fp64_peak, "ops_per_launch": ops}
+        if fp64_line is not None:
+            fp64_line["ratio"] = value / fp64_line["value"]
+            line["fp64_gpu"] = fp64_line
+        if pos_err is not None:
+            line["pos_err"] = pos_err
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(scenes, cfgs, sub, args.cpu_sample_seconds)
         print(json.dumps(line), flush=True)
