@@ -200,9 +200,9 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   if (denseKind == 2) {
     deltaSmem(I, teamCtas, &I.denseResRows);
     teamCaps(I, teamCtas, &I.teamECap, &I.teamBCap);
-    I.oRtag = A.zeros(8 * 3 * n);
+    I.oRtag = A.zeros(8 * 2 * 3 * n);  // two buffers
     I.oXtag = A.zeros(8 * 6 * n);
-    I.oPtag = A.zeros(8 * 2 * 16 * static_cast<size_t>(teamCtas));  // one 128-byte line per partial
+    I.oPtag = A.zeros(8 * 3 * 16 * static_cast<size_t>(teamCtas));  // A (two buffers), B; a line each
     I.oEpoch = A.zeros(4);
     I.oErr = A.zeros(4);
     // positions a CTA reads: its vertices, their edge neighbours and bend-stencil partners
@@ -548,7 +548,7 @@ struct pd_sim {
     const int count = static_cast<int>(inst.size());
     const int want = inst[0].cfg.cluster_ctas;
     int team = want > 0 ? want : sms / count;
-    team = std::min({team, sms / count, minN, 256});  // 256: flags one polling warp covers
+    team = std::min({team, sms / count, minN, 256});  // 256: partials one polling warp covers
     if (team < 2) return false;
     int smem = 0, rows = 0;
     for (const auto& I : inst) smem = std::max(smem, deltaSmem(I, team, &rows));
@@ -638,8 +638,8 @@ struct pd_sim {
     for (const auto& I : inst) {
       PD_CUDA(cudaMemset(dArena + I.oErr, 0, 4));
       PD_CUDA(cudaMemset(dArena + I.oEpoch, 0, 4));
-      PD_CUDA(cudaMemset(dArena + I.oPtag, 0, 8 * 2 * 16 * static_cast<size_t>(teamCtas)));
-      PD_CUDA(cudaMemset(dArena + I.oRtag, 0, 8 * 3 * static_cast<size_t>(I.scene.n)));
+      PD_CUDA(cudaMemset(dArena + I.oPtag, 0, 8 * 3 * 16 * static_cast<size_t>(teamCtas)));
+      PD_CUDA(cudaMemset(dArena + I.oRtag, 0, 8 * 2 * 3 * static_cast<size_t>(I.scene.n)));
       PD_CUDA(cudaMemset(dArena + I.oXtag, 0, 8 * 6 * static_cast<size_t>(I.scene.n)));
     }
     return fail(PD_ERR_CUDA, "a team exchange of the substep kernel gave up waiting; the state is undefined");

@@ -103,9 +103,9 @@ struct InstanceDev {
   const int4* tBend;           // per bend incidence (bstart order): a, b, c (| pinned << 31), (−k)·w_v bits
   const float4* tVtx;          // per vertex: m/h², 1/m (0 when m ≤ 0), pinned, 0
   const float4* qhl;           // per vertex: pin position as hi (x, y, z, 0), lo (x, y, z, 0)
-  unsigned long long* rtag;    // 3n words: correction b − Ã·x, component-major
+  unsigned long long* rtag;    // 2 × 3n words: correction b − Ã·x, component-major, two buffers
   unsigned long long* xtag;    // 6n words: positions as hi x, y, z, lo x, y, z (x = hi + lo)
-  unsigned long long* ptag;    // 2 × team × 16 words: per-CTA partial maxima of the two exchanges
+  unsigned long long* ptag;    // 3 × team × 16 words: per-CTA partial maxima (A in two buffers, B)
   uint32_t* epoch;             // last exchange epoch of the previous launch
   const int32_t* window;       // 2 × team: vertex range [lo, hi) whose positions a CTA reads
   int32_t* err;                // set when an exchange gave up waiting

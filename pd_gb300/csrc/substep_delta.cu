@@ -26,11 +26,13 @@
 // relaxed gpu-scope accesses: a reader polls the words it needs until each carries the current
 // epoch, so an exchange costs about one L2 round trip after the last writer and needs no fence
 // (a fence would also drop the L1 lines the CTA reads through). Per-CTA partial maxima (residual,
-// displacement, scale) travel the same way, one per L2 line; one warp polls them first and the
-// data words are read once every CTA has published, which keeps waiting CTAs from flooding L2. A word is rewritten only two exchanges later, which
-// no CTA reaches before every CTA has read it. The launch is cooperative so that every CTA of the
-// team is resident, and every poll gives up after a bounded number of rounds, setting the
-// instance's error flag.
+// displacement, scale) travel the same way, one per L2 line; one warp polls them while the
+// others poll the data words, backing off between rounds so that waiting CTAs do not flood L2.
+// Exchange A is a full barrier of the team; with the residual gate exchange B only waits for
+// the CTAs whose positions a CTA reads, so r and the A partials alternate between two buffers.
+// Every word is rewritten only after a later full barrier, which no CTA passes before every CTA
+// has read it. The launch is cooperative so that every CTA of the team is resident, and every
+// poll gives up after a bounded number of rounds, setting the instance's error flag.
 #include <cstdint>
 
 #include "device.cuh"
@@ -71,6 +73,7 @@ __device__ __forceinline__ bool pollWords(const unsigned long long* src, int b, 
     for (int u = 0; u < B; ++u)
       if (j0 + u * nth < e) pending |= 1u << u;
     long long spins = 0;
+    unsigned nap = 32;  // back off while words are stale, so waiting CTAs do not flood L2
     while (pending) {
       unsigned long long w[B];
 #pragma unroll
@@ -82,7 +85,11 @@ __device__ __forceinline__ bool pollWords(const unsigned long long* src, int b, 
           pending &= ~(1u << u);
         }
       }
-      if (pending && ++spins > kSpinLimit) return false;
+      if (pending) {
+        if (++spins > kSpinLimit) return false;
+        __nanosleep(nap);
+        nap = min(2 * nap, 256u);
+      }
     }
   }
   return true;
@@ -94,22 +101,25 @@ __device__ __forceinline__ float warpMaxF(float v) {
   return v;
 }
 
-// Warp 0: maximum of the team's partials tagged `tag` into *out (other warps return true).
-__device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int team, unsigned tag, float* out) {
+// Warp 0: maximum of the partials tagged `tag` of the team's ranks r ≡ first (mod step) into
+// *out (other warps return true).
+__device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int team, unsigned tag, float* out,
+                                             int first = 0, int step = 1) {
   if (threadIdx.x >= 32) return true;
   const int lane = threadIdx.x;
   unsigned pending = 0;
 #pragma unroll
   for (int i = 0; i < kMaxTeam / 32; ++i)
-    if (lane + 32 * i < team) pending |= 1u << i;
+    if (first + step * (lane + 32 * i) < team) pending |= 1u << i;
   float mx = 0.f;
   long long spins = 0;
+  unsigned nap = 32;
   bool good = true;
   while (true) {
     unsigned long long w[kMaxTeam / 32];
 #pragma unroll
     for (int i = 0; i < kMaxTeam / 32; ++i)
-      w[i] = ((pending >> i) & 1u) ? loadRelaxed(ptag + kPartStride * (lane + 32 * i)) : 0ull;
+      w[i] = ((pending >> i) & 1u) ? loadRelaxed(ptag + kPartStride * (first + step * (lane + 32 * i))) : 0ull;
 #pragma unroll
     for (int i = 0; i < kMaxTeam / 32; ++i) {
       if (((pending >> i) & 1u) && static_cast<unsigned>(w[i] >> 32) == tag) {
@@ -122,6 +132,8 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
       good = false;
       break;
     }
+    __nanosleep(nap);
+    nap = min(2 * nap, 256u);
   }
   mx = warpMaxF(mx);
   if (lane == 0) *out = mx;
@@ -269,8 +281,9 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     for (int t = threadIdx.x; t < total; t += blockDim.x) dst[t] = __ldg(src + t);
   }
   unsigned epoch = *I.epoch;  // exchanges of this launch continue the previous launch's epochs
-  unsigned long long* ptagA = I.ptag;
-  unsigned long long* ptagB = I.ptag + kPartStride * team;
+  // exchange words: r and the A partials alternate between two buffers (by A epoch), since with
+  // the residual gate exchange B only waits for the CTAs whose positions a CTA reads
+  unsigned long long* ptagB = I.ptag + 2 * kPartStride * team;
   const int wlo = I.window[2 * rank], whi = I.window[2 * rank + 1];
   // GEMV work: row pairs × column segments over the warps
   const int pairs = (m + 1) / 2;
@@ -300,7 +313,10 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
     for (int k = 0;; ++k) {
-      const unsigned tagA = ++epoch;
+      const unsigned tagA = ++epoch;  // odd: epochs are consumed in (A, B) pairs
+      const unsigned buf = (tagA >> 1) & 1u;
+      unsigned long long* rtag = I.rtag + buf * 3 * n;
+      unsigned long long* ptagA = I.ptag + buf * kPartStride * team;
       // correction r and residual of x^k for own vertices, kGroup lanes per vertex (FP32 only)
       float resLocal = 0.f;
       const int gl = threadIdx.x & (kGroup - 1), group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
@@ -389,13 +405,13 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
             r1 = (f1 - a1) - p1;
             r2 = (f2 - a2) - p2;
           }
-          storeRelaxed(I.rtag + v, tagged(tagA, r0));
-          storeRelaxed(I.rtag + n + v, tagged(tagA, r1));
-          storeRelaxed(I.rtag + 2 * n + v, tagged(tagA, r2));
+          storeRelaxed(rtag + 3 * v, tagged(tagA, r0));
+          storeRelaxed(rtag + 3 * v + 1, tagged(tagA, r1));
+          storeRelaxed(rtag + 3 * v + 2, tagged(tagA, r2));
         }
       }
-      // exchange A: the whole correction (warps 1..), the maximum of the residuals — at k = 0 of
-      // the scale — (warp 0)
+      // exchange A, a full barrier of the team: the whole correction (warps 1..) and the maximum
+      // of the residuals — at k = 0 of the scale — (warp 0)
       resLocal = warpMaxF(resLocal);
       if (lane == 0) red[warp] = (k == 0) ? scW : resLocal;
       __syncthreads();
@@ -408,26 +424,28 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
+      } else {
+        ok = pollWords<10>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
+          const int v = j / 3;
+          Rs[(j - 3 * v) * ld + v] = val;
+        });
       }
-      if (!ok) failed = 1;
-      __syncthreads();  // every CTA has published: the words below are (almost always) current
-      if (failed) break;
-      ok = pollWords<10>(I.rtag, 0, 3 * n, tagA, threadIdx.x, blockDim.x, [&](int j, float val) {
-        const int c = j / n;
-        Rs[c * ld + (j - c * n)] = val;
-      });
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
       const double gateA = gate;
       if (k == 0) scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
+      bool stop = k == I.maxIter;
       if (I.useResidual && k >= 1) {
         lastRes = gateA;
         used = k;
         conv = gateA <= I.resThreshold;
-        if (conv) break;
+        stop = stop || conv;
       }
-      if (k == I.maxIter) break;
+      if (stop) {
+        ++epoch;  // the unused B epoch: the next A epoch stays odd
+        break;
+      }
 
       // this CTA's rows of Ã⁻¹·r: row pairs × column segments over the warps
       for (int task = warp; task < pairs * segs; task += kWarps) {
@@ -465,27 +483,34 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         storeRelaxed(I.xtag + 6 * v + c, tagged(tagB, hi));
         storeRelaxed(I.xtag + 6 * v + 3 + c, tagged(tagB, lo));
       }
-      // exchange B: the positions this CTA reads (warps 1..), the maximum of the displacements
-      // (warp 0)
-      dmax = warpMaxF(dmax);
-      if (lane == 0) red[warp] = dmax;
-      __syncthreads();
-      if (warp == 0) {
-        if (lane == 0) {
-          float pm = 0.f;
-          for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
-          storeRelaxed(ptagB + kPartStride * rank, tagged(tagB, pm));
+      // exchange B: the positions this CTA reads; with the displacement gate also the maximum of
+      // the displacements (warp 0), which makes it a full barrier — with the residual gate a CTA
+      // waits only for the CTAs owning its window
+      __syncthreads();  // own positions are read back by other threads below
+      if (!I.useResidual) {
+        dmax = warpMaxF(dmax);
+        if (lane == 0) red[warp] = dmax;
+        __syncthreads();
+        if (warp == 0) {
+          if (lane == 0) {
+            float pm = 0.f;
+            for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
+            storeRelaxed(ptagB + kPartStride * rank, tagged(tagB, pm));
+          }
+          __syncwarp();
+          ok = pollPartials(ptagB, team, tagB, &gate);
+        } else {
+          ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
+            const int v = j / 6, c = j - 6 * v;  // c < 3: hi, else lo
+            xf[8 * v + (c < 3 ? c : c + 1)] = val;
+          });
         }
-        __syncwarp();
-        ok = pollPartials(ptagB, team, tagB, &gate);
+      } else {
+        ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x, blockDim.x, [&](int j, float val) {
+          const int v = j / 6, c = j - 6 * v;
+          xf[8 * v + (c < 3 ? c : c + 1)] = val;
+        });
       }
-      if (!ok) failed = 1;
-      __syncthreads();
-      if (failed) break;
-      ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x, blockDim.x, [&](int j, float val) {
-        const int v = j / 6, c = j - 6 * v;  // c < 3: hi, else lo
-        xf[8 * v + (c < 3 ? c : c + 1)] = val;
-      });
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
