@@ -175,7 +175,9 @@ typedef struct pd_sim_info {
 #define PD_SOLVE_SUPERNODAL32 2  /* FP32 supernodes + one FP64 refinement step */
 #define PD_SOLVE_DENSE32 3       /* explicit FP32 inverse + one FP64 refinement step */
 #define PD_SOLVE_DENSE32_TEAM 4  /* MIXED: explicit FP32 inverse applied to the correction b − Ã·x
-                                    by a team of co-resident CTAs per cloth (FP64 positions) */
+                                    by a team of co-resident CTAs per cloth */
+#define PD_SOLVE_SUPERNODAL32_CORRECTION 5 /* MIXED: FP32 supernodes applied to the correction
+                                              b − Ã·x, one CTA per cloth */
 
 typedef struct pd_sim_stats {    /* SimContext counters (core/sim/Scene.h:161-169) */
   int32_t iterations_used;       /* of the last substep */

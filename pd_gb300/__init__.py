@@ -15,6 +15,7 @@ from .api import (  # noqa: F401
     PD_SOLVE_SUPERNODAL32,
     PD_SOLVE_DENSE32,
     PD_SOLVE_DENSE32_TEAM,
+    PD_SOLVE_SUPERNODAL32_CORRECTION,
     PdError,
     SceneConfig,
     GridScene,

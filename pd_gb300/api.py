@@ -26,6 +26,7 @@ PD_SOLVE_SUPERNODAL = 1
 PD_SOLVE_SUPERNODAL32 = 2
 PD_SOLVE_DENSE32 = 3
 PD_SOLVE_DENSE32_TEAM = 4
+PD_SOLVE_SUPERNODAL32_CORRECTION = 5
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpd_gb300.so")

@@ -25,6 +25,7 @@ UNITS = {
     "substep_fast.cu": [],
     "substep_mixed.cu": [],
     "substep_delta.cu": [],
+    "substep_corr.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
 }
 

@@ -93,7 +93,8 @@ struct Instance {
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
       oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
-      oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl;
+      oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl, oXhl,
+      oXhatHl;
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
   int teamECap = 0, teamBCap = 0;
@@ -180,7 +181,8 @@ int deltaSmem(const Instance& I, int team, int* resRows) {
   return static_cast<int>(fixed + 4L * rows * ld);
 }
 
-// kind: 0 none, 1 dense inverse (cluster kernel), 2 dense inverse + team kernel buffers
+// kind: 0 none, 1 dense inverse (cluster kernel), 2 dense inverse + team kernel buffers,
+// 3 FP32 tables + position pairs of the one-CTA correction kernel
 void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
@@ -190,8 +192,9 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.denseResRows = 0;
   I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
   I.oRtag = I.oXtag = I.oPtag = I.oEpoch = I.oWindow = I.oErr = I.oTEdge = I.oTBend = I.oTVtx = I.oQhl = 0;
+  I.oXhl = I.oXhatHl = 0;
   I.teamECap = I.teamBCap = 0;
-  if (denseKind > 0) {
+  if (denseKind == 1 || denseKind == 2) {
     I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
     I.oVcol = A.add(I.L.col);
@@ -228,7 +231,9 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
       window[2 * r + 1] = hi;
     }
     I.oWindow = A.add(window);
-    // incidences in the kernel's FP32 form (pinned endpoints flagged in bit 31)
+  }
+  if (denseKind >= 2) {
+    // incidences in the kernels' FP32 form (pinned endpoints flagged in bit 31)
     auto bitsOf = [](float f) {
       int32_t i;
       std::memcpy(&i, &f, 4);
@@ -264,6 +269,10 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
     I.oTBend = A.add(tb);
     I.oTVtx = A.add(tv);
     I.oQhl = A.add(pinPairs(s));
+    if (denseKind == 3) {
+      I.oXhl = A.zeros(32 * n);
+      I.oXhatHl = A.zeros(32 * n);
+    }
   }
   I.oX = A.add(s.x);
   I.oV = A.add(s.v);
@@ -435,13 +444,19 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
     d.Vval = reinterpret_cast<const double*>(P(I.oVval));
   }
   d.denseResRows = I.denseResRows;
-  if (I.oRtag) {
-    d.teamECap = I.teamECap;
-    d.teamBCap = I.teamBCap;
+  if (I.oTEdge) {
     d.tEdge = reinterpret_cast<const int4*>(P(I.oTEdge));
     d.tBend = reinterpret_cast<const int4*>(P(I.oTBend));
     d.tVtx = reinterpret_cast<const float4*>(P(I.oTVtx));
     d.qhl = reinterpret_cast<const float4*>(P(I.oQhl));
+  }
+  if (I.oXhl) {
+    d.xhl = reinterpret_cast<float*>(P(I.oXhl));
+    d.xhathl = reinterpret_cast<float*>(P(I.oXhatHl));
+  }
+  if (I.oRtag) {
+    d.teamECap = I.teamECap;
+    d.teamBCap = I.teamBCap;
     d.rtag = reinterpret_cast<unsigned long long*>(P(I.oRtag));
     d.xtag = reinterpret_cast<unsigned long long*>(P(I.oXtag));
     d.ptag = reinterpret_cast<unsigned long long*>(P(I.oPtag));
@@ -476,6 +491,7 @@ struct pd_sim {
   uint8_t* dArena = nullptr;
   size_t arenaBytes = 0;
   pdg::InstanceDev* dDesc = nullptr;
+  pdg::InstanceDev* dDescOrder = nullptr;  // batch descriptors by decreasing cost (correction kernel)
   int32_t* dIterLog = nullptr;
   uint8_t* dConvLog = nullptr;
   int logCapacity = 0;
@@ -484,6 +500,7 @@ struct pd_sim {
   int teamCtas = 1;  // CTAs per instance (a thread-block cluster when > 1)
   bool dense = false;  // mixed modes: the cluster applies the explicit FP32 inverse
   bool delta = false;  // MIXED: a team of co-resident CTAs per cloth, correction-form dense solve
+  bool corr = false;   // MIXED above the dense limit: one CTA per cloth, correction-form FP32 solve
 
   ~pd_sim() { release(); }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
@@ -501,8 +518,12 @@ struct pd_sim {
     teamCtas = 1;
     dense = false;
     delta = false;
+    corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
-    if (p == PD_PRECISION_MIXED && planDelta()) return;
+    if (p == PD_PRECISION_MIXED) {
+      if (!planDelta()) corr = true;
+      return;
+    }
     int want = inst[0].cfg.cluster_ctas;
     if (want <= 0) {
       const int count = static_cast<int>(inst.size());
@@ -569,10 +590,12 @@ struct pd_sim {
   void release() {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
+    if (dDescOrder) cudaFree(dDescOrder);
     if (dIterLog) cudaFree(dIterLog);
     if (dConvLog) cudaFree(dConvLog);
     dArena = nullptr;
     dDesc = nullptr;
+    dDescOrder = nullptr;
     dIterLog = nullptr;
     dConvLog = nullptr;
     logCapacity = 0;
@@ -581,7 +604,7 @@ struct pd_sim {
   int upload(int capacity) {
     Arena A;
     planTeam();
-    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : dense ? 1 : 0);
+    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : corr ? 3 : dense ? 1 : 0);
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -613,12 +636,33 @@ struct pd_sim {
       int rows = 0;
       const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
                        : dense ? denseSmem(inst[i].scene.n)
+                       : corr  ? 24 * inst[i].scene.n
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
-      if ((delta || need <= kMaxSmem) && need > smem) smem = need;
+      // the correction kernel keeps its solve vectors in shared memory up to 48 KB, so that a
+      // batch still runs four CTAs per SM
+      const int cap = corr ? 48 * 1024 : kMaxSmem;
+      if ((delta || need <= cap) && need > smem) smem = need;
     }
     smemBytes = smem;
     if (!dDesc) PD_CUDA(cudaMalloc(&dDesc, sizeof(pdg::InstanceDev) * inst.size()));
     PD_CUDA(cudaMemcpy(dDesc, desc.data(), sizeof(pdg::InstanceDev) * desc.size(), cudaMemcpyHostToDevice));
+    if (corr && inst.size() > 1) {  // launch order of the one-CTA kernel: most expensive first
+      std::vector<size_t> order(inst.size());
+      for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+      auto cost = [&](size_t i) {
+        const Instance& I = inst[i];
+        return static_cast<double>(I.F.colval.size()) + 8.0 * I.scene.edges.size() + 4.0 * I.scene.n;
+      };
+      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost(a) > cost(b); });
+      std::vector<pdg::InstanceDev> sorted;
+      for (size_t i : order) sorted.push_back(desc[i]);
+      if (!dDescOrder) PD_CUDA(cudaMalloc(&dDescOrder, sizeof(pdg::InstanceDev) * inst.size()));
+      PD_CUDA(cudaMemcpy(dDescOrder, sorted.data(), sizeof(pdg::InstanceDev) * sorted.size(),
+                         cudaMemcpyHostToDevice));
+    } else if (dDescOrder) {
+      cudaFree(dDescOrder);
+      dDescOrder = nullptr;
+    }
     return PD_OK;
   }
 
@@ -916,6 +960,8 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
     rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
   } else if (s->delta) {
     rc = pdg::launchSubstepDelta(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
+  } else if (s->corr) {
+    rc = pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes, s->stream);
   } else if (s->dense) {
     rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (mixedSolve(p)) {
@@ -1078,6 +1124,7 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                     : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
                     : s->delta                   ? PD_SOLVE_DENSE32_TEAM
+                    : s->corr                    ? PD_SOLVE_SUPERNODAL32_CORRECTION
                     : s->dense                   ? PD_SOLVE_DENSE32
                                                  : PD_SOLVE_SUPERNODAL32;
   return PD_OK;

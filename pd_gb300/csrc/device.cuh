@@ -103,6 +103,8 @@ struct InstanceDev {
   const int4* tBend;           // per bend incidence (bstart order): a, b, c (| pinned << 31), (−k)·w_v bits
   const float4* tVtx;          // per vertex: m/h², 1/m (0 when m ≤ 0), pinned, 0
   const float4* qhl;           // per vertex: pin position as hi (x, y, z, 0), lo (x, y, z, 0)
+  float* xhl;                  // 8n: positions as pairs (one-CTA correction kernel)
+  float* xhathl;               // 8n: x̂ as pairs (one-CTA correction kernel)
   unsigned long long* rtag;    // 2 × 3n words: correction b − Ã·x, component-major, two buffers
   unsigned long long* xtag;    // 6n words: positions as hi x, y, z, lo x, y, z (x = hi + lo)
   unsigned long long* ptag;    // 3 × team × 16 words: per-CTA partial maxima (A in two buffers, B)
@@ -148,6 +150,9 @@ int denseClusterSupported(int clusterSize, int smemBytes);
 int launchSubstepDelta(const InstanceDev* dInstances, int count, int team, int smemBytes, int substeps, void* stream);
 // CTAs of kDeltaThreads threads with smemBytes each that can be co-resident on the device.
 int deltaResidentCtas(int smemBytes);
+// MIXED substep for cloths above the explicit-inverse limit, one CTA per instance: x ← x +
+// L⁻¹·(b − Ã·x) with the FP32 supernodal solve (smemBytes: 24·n when the solve vectors fit).
+int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
 constexpr int kDeltaThreads = 512;
 
 constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and

@@ -35,6 +35,7 @@
 // poll gives up after a bounded number of rounds, setting the instance's error flag.
 #include <cstdint>
 
+#include "correction.cuh"
 #include "device.cuh"
 
 namespace pdg {
@@ -151,33 +152,6 @@ __device__ __forceinline__ double warpMaxD(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
-}
-
-// FP64 value as an FP32 pair with hi + lo = v to ~2⁻⁴⁸ relative.
-__device__ __forceinline__ void split(double v, float& hi, float& lo) {
-  hi = static_cast<float>(v);
-  lo = static_cast<float>(v - static_cast<double>(hi));
-}
-
-// Difference of two positions held as hi/lo pairs, to FP32 rounding of the result.
-__device__ __forceinline__ float3 diffHL(float4 ah, float4 al, float4 bh, float4 bl) {
-  return make_float3((ah.x - bh.x) + (al.x - bl.x), (ah.y - bh.y) + (al.y - bl.y), (ah.z - bh.z) + (al.z - bl.z));
-}
-
-// Pin position q_u as the hi/lo pair the host split it into.
-__device__ __forceinline__ void pinHL(const InstanceDev& I, int u, float4& h, float4& l) {
-  h = __ldg(I.qhl + 2 * u);
-  l = __ldg(I.qhl + 2 * u + 1);
-}
-
-// (hi, lo) + d as a renormalised pair: Knuth's two-sum of hi and d, then a fast two-sum.
-__device__ __forceinline__ void addHL(float& hi, float& lo, float d) {
-  const float s = hi + d;
-  const float bb = s - hi;
-  const float e = (hi - (s - bb)) + (d - bb);
-  const float l = lo + e;
-  hi = s + l;
-  lo = l - (hi - s);
 }
 
 // Rows of Ã⁻¹ times the three components of R over the float4 columns [jb, je), two rows per
@@ -325,89 +299,22 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         const bool active = li < m;
         const float4 vc = active ? sV[li] : make_float4(0.f, 0.f, 1.f, 0.f);
         const int v = rb + li;
-        // a: mass + edge terms of the residual, f: its bend terms, p: what the matrix adds to
-        // f − a because it couples pinned neighbours at q rather than at their positions
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f, p0 = 0.f, p1 = 0.f, p2 = 0.f;
+        CorrectionSums cs;
         if (vc.z == 0.f) {
           const float4 vh = Xs[2 * v], vl = Xs[2 * v + 1];
-          for (int q = sEb[li] + gl; q < sEb[li + 1]; q += kGroup) {
-            const int4 E = sE[q];
-            const int o = E.x & 0x7fffffff;
-            const float rest = __int_as_float(E.y), kap = __int_as_float(E.z);
-            const float3 rel = diffHL(vh, vl, Xs[2 * o], Xs[2 * o + 1]);  // x_v − x_o
-            const float len = sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
-            float dx = 0.f, dy = 0.f, dz = 0.f;
-            if (!(len <= 1e-12f)) {
-              const float s = rest / len;
-              dx = rel.x * s;
-              dy = rel.y * s;
-              dz = rel.z * s;
-            }
-            // ±rc_e = κ·(x_a − x_b) − κ·d_e seen from v (the projection is odd in x_a − x_b)
-            a0 = fmaf(kap, rel.x - dx, a0);
-            a1 = fmaf(kap, rel.y - dy, a1);
-            a2 = fmaf(kap, rel.z - dz, a2);
-            if (E.x < 0) {  // pinned neighbour: the matrix sees it at q
-              float4 qh, ql;
-              pinHL(I, o, qh, ql);
-              const float3 relq = diffHL(vh, vl, qh, ql);
-              p0 = fmaf(kap, relq.x - rel.x, p0);
-              p1 = fmaf(kap, relq.y - rel.y, p1);
-              p2 = fmaf(kap, relq.z - rel.z, p2);
-            }
-          }
-          for (int q = sBb[li] + gl; q < sBb[li + 1]; q += kGroup) {
-            const int4 S = sB[q];
-            const int a = S.x & 0x7fffffff, b = S.y & 0x7fffffff, c = S.z & 0x7fffffff;
-            const float fac = __int_as_float(S.w);
-            float4 ah = Xs[2 * a], al = Xs[2 * a + 1], bh = Xs[2 * b], bl = Xs[2 * b + 1], ch = Xs[2 * c],
-                   cl = Xs[2 * c + 1];
-            const float3 u = diffHL(ah, al, bh, bl), w = diffHL(ch, cl, bh, bl);
-            f0 = fmaf(fac, u.x + w.x, f0);
-            f1 = fmaf(fac, u.y + w.y, f1);
-            f2 = fmaf(fac, u.z + w.z, f2);
-            if ((S.x | S.y | S.z) < 0) {  // pinned members: the matrix part sees them at q
-              if (S.x < 0) pinHL(I, a, ah, al);
-              if (S.y < 0) pinHL(I, b, bh, bl);
-              if (S.z < 0) pinHL(I, c, ch, cl);
-              const float3 uq = diffHL(ah, al, bh, bl), wq = diffHL(ch, cl, bh, bl);
-              p0 = fmaf(fac, (u.x + w.x) - (uq.x + wq.x), p0);
-              p1 = fmaf(fac, (u.y + w.y) - (uq.y + wq.y), p1);
-              p2 = fmaf(fac, (u.z + w.z) - (uq.z + wq.z), p2);
-            }
-          }
-          if (gl == 0) {  // mass term (x − x̂)·m/h²
-            const float3 dx = diffHL(vh, vl, sXh[2 * li], sXh[2 * li + 1]);
-            a0 = fmaf(dx.x, vc.x, a0);
-            a1 = fmaf(dx.y, vc.x, a1);
-            a2 = fmaf(dx.z, vc.x, a2);
-          }
+          cs.accumulate(I, sE, sEb[li], sEb[li + 1], sB, sBb[li], sBb[li + 1], Xs, vh, vl, gl, kGroup);
+          if (gl == 0) cs.addMass(vh, vl, sXh[2 * li], sXh[2 * li + 1], vc.x);
         }
-        a0 = groupSum<kGroup>(a0);
-        a1 = groupSum<kGroup>(a1);
-        a2 = groupSum<kGroup>(a2);
-        f0 = groupSum<kGroup>(f0);
-        f1 = groupSum<kGroup>(f1);
-        f2 = groupSum<kGroup>(f2);
-        p0 = groupSum<kGroup>(p0);
-        p1 = groupSum<kGroup>(p1);
-        p2 = groupSum<kGroup>(p2);
+        cs.reduce<kGroup>();
         if (active && gl == 0) {
-          float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+          float3 r = make_float3(0.f, 0.f, 0.f);
           if (vc.z == 0.f) {
-            if (vc.y > 0.f) {
-              const float t0 = a0 + f0, t1 = a1 + f1, t2 = a2 + f2;
-              resLocal = fmaxf(resLocal, sqrtf(t0 * t0 + t1 * t1 + t2 * t2) * vc.y);
-            }
-            // r = −(mass + edge terms) + bend terms with pinned neighbours at q (the pinned part
-            // of the bend terms is the reference's constant bending RHS)
-            r0 = (f0 - a0) - p0;
-            r1 = (f1 - a1) - p1;
-            r2 = (f2 - a2) - p2;
+            if (vc.y > 0.f) resLocal = fmaxf(resLocal, cs.residual(vc.y));
+            r = cs.correction();
           }
-          storeRelaxed(rtag + 3 * v, tagged(tagA, r0));
-          storeRelaxed(rtag + 3 * v + 1, tagged(tagA, r1));
-          storeRelaxed(rtag + 3 * v + 2, tagged(tagA, r2));
+          storeRelaxed(rtag + 3 * v, tagged(tagA, r.x));
+          storeRelaxed(rtag + 3 * v + 1, tagged(tagA, r.y));
+          storeRelaxed(rtag + 3 * v + 2, tagged(tagA, r.z));
         }
       }
       // exchange A, a full barrier of the team: the whole correction (warps 1..) and the maximum

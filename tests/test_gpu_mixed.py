@@ -33,11 +33,12 @@ def with_mode(cfg, mode, ctas=0, dense=0):
 
 
 def expected_kind(pdg, mode, ctas, dense):
-    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION:
+    m = MODES[mode]
+    if m == pdg.PD_PRECISION_FP32_PROJECTION:
         return pdg.PD_SOLVE_SUPERNODAL
-    if ctas == 1 or dense < 0:
-        return pdg.PD_SOLVE_SUPERNODAL32
-    return pdg.PD_SOLVE_DENSE32_TEAM if MODES[mode] == pdg.PD_PRECISION_MIXED else pdg.PD_SOLVE_DENSE32
+    if m == pdg.PD_PRECISION_MIXED:  # a team on the explicit inverse, else one CTA in correction form
+        return pdg.PD_SOLVE_DENSE32_TEAM if (ctas != 1 and dense >= 0) else pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
+    return pdg.PD_SOLVE_SUPERNODAL32 if (ctas == 1 or dense < 0) else pdg.PD_SOLVE_DENSE32
 
 
 @pytest.mark.parametrize("mode", list(MODES))
@@ -87,12 +88,13 @@ def test_batch_mixed(pdg, dense):
 
 
 def test_large_cloth_uses_global_workspace(pdg):
-    """A 90×90 cloth does not fit the shared-memory workspace: one CTA with L2 workspaces."""
+    """A 90×90 cloth is above the explicit-inverse limit and its solve vectors do not fit shared
+    memory: one CTA in correction form with L2 workspaces."""
     cfg = with_mode(W._base(grid_nx=90, grid_ny=90, grid_spacing=1 / 89, max_iterations=10,
                             shear_stiffness=1000.0), "mixed")
     scene = pdg.make_grid(cfg)
     sim = pdg.Simulator(scene, cfg)
-    assert sim.info()["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32
+    assert sim.info()["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
     orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
     sim.step(30)
     orc.step(30)
@@ -162,3 +164,36 @@ def test_team_batch_and_repeated_launches(pdg):
         orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
         orc.step(50)
         assert max_rel(sim.state(i)[0], orc.state()[0]) < TOL_POS, i
+
+
+@pytest.mark.parametrize("strategy", ["one-cta", "cluster-supernodal"])
+def test_correction_gates_and_pins(pdg, strategy):
+    """One-CTA correction kernel: residual gate that fires, displacement gate, zero iterations,
+    and pin drags."""
+    ctas, dense = STRATEGIES[strategy]
+    cases = [
+        W._base(grid_nx=12, grid_ny=12, grid_spacing=0.05, max_iterations=30, residual_tolerance=0.3,
+                velocity_damping=0.02),
+        W._base(grid_nx=10, grid_ny=14, grid_spacing=0.05, max_iterations=25, residual_tolerance=0.0,
+                rel_tolerance=5e-2),
+        W._base(grid_nx=10, grid_ny=10, grid_spacing=0.05, max_iterations=0),
+    ]
+    for cfg in cases:
+        scene = pdg.make_grid(cfg)
+        sim = pdg.Simulator(scene, with_mode(cfg, "mixed", ctas, dense))
+        assert sim.info()["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
+        orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+        sim.step(60)
+        it_o, cv_o = orc.step(60)
+        if cfg.max_iterations:
+            pins = np.flatnonzero(scene.pinned)
+            q = scene.positions.copy()
+            q[pins, 0] += 0.03
+            sim.set_pin_positions(q)
+            orc.set_pin_positions(q)
+            sim.step(40)
+            it2, cv2 = orc.step(40)
+            it_o, cv_o = np.concatenate([it_o, it2]), np.concatenate([cv_o, cv2])
+        assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
+        it_g, cv_g = sim.iteration_log()
+        assert np.mean(it_g == it_o[-len(it_g):]) > 0.95
