@@ -223,6 +223,19 @@ int pd_sim_get_factor(pd_sim* s, int32_t instance, int32_t* perm, int32_t* colpt
 /* Runs one 3-column solve with the instance's factor: b, x host arrays of 3n. */
 int pd_sim_solve(pd_sim* s, int32_t instance, const double* b, double* x);
 
+/* ---- Differentiation (no counterpart in the reference) ----
+ * For every instance i: the loss L_i = mean over free vertices of |x − targets[i]|² after
+ * `substeps` substeps from the current state, with the iteration count fixed at max_iterations
+ * (the convergence gate is not differentiated) and an external per-vertex force forces[i] (3n,
+ * NULL = 0) entering the prediction as x̂ = x + h·v + h²·g + h²·f/m; and, by the adjoint method in
+ * FP64 with per-substep checkpoints, its gradient w.r.t. the per-edge stiffness (dkappa[i], n_edges),
+ * the current velocities (dv0[i], 3n) and the force (dforce[i], 3n). All arrays are host memory,
+ * one pointer per instance; loss may be NULL, and an instance whose three gradient pointers are
+ * NULL gets its loss only. The state is left unchanged. One CTA per instance; a batch of problems
+ * runs in one launch. Blocks until the results are copied back. */
+int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, const double* const* forces,
+                    double* loss, double* const* dkappa, double* const* dv0, double* const* dforce);
+
 /* ---- Host-only inspection (no GPU work): the preparation pd_sim_create performs ---- */
 /* Assembles L, orders and factorizes as pd_sim_create does; exports the factor like
  * pd_sim_get_factor (call once with NULL arrays to read *nnz) and fills *info (nullable). */

@@ -97,6 +97,8 @@ def lib():
     L.oracle_sim_coloring.restype = C.c_int
     L.oracle_sim_bend_rhs.argtypes = [C.c_void_p, dp]
     L.oracle_project_one.argtypes = [dp, dp, C.c_double, dp]
+    L.oracle_sim_gradient.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp]
+    L.oracle_sim_gradient.restype = C.c_int
     _lib = L
     return L
 
@@ -290,6 +292,23 @@ class OracleSim:
         if self._L.oracle_sim_solve(self._h, _ptr(b, C.c_double), _ptr(x, C.c_double)) != 0:
             raise RuntimeError("factorization failed")
         return x.reshape(-1, 3)
+
+    def gradient(self, substeps, targets, force=None, grad=True):
+        """Loss (mean over free vertices of |x − target|² after `substeps` substeps with the
+        iteration count fixed) and, if `grad`, its gradient w.r.t. per-edge stiffness, initial
+        velocities and an external per-vertex force; the state is left unchanged."""
+        t = np.ascontiguousarray(targets, np.float64).reshape(-1)
+        f = None if force is None else np.ascontiguousarray(force, np.float64).reshape(-1)
+        loss = C.c_double()
+        dk = np.zeros(self.n_edges) if grad else None
+        dv = np.zeros((self.n, 3)) if grad else None
+        df = np.zeros((self.n, 3)) if grad else None
+        rc = self._L.oracle_sim_gradient(self._h, int(substeps), _ptr(t, C.c_double), _ptr(f, C.c_double),
+                                         C.byref(loss), _ptr(dk, C.c_double), _ptr(dv, C.c_double),
+                                         _ptr(df, C.c_double))
+        if rc != 0:
+            raise RuntimeError("oracle gradient failed")
+        return dict(loss=loss.value, dkappa=dk, dv0=dv, dforce=df)
 
     def rhs(self, base, overwrite_pins=True):
         base = np.ascontiguousarray(base, np.float64).reshape(-1)

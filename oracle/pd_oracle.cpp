@@ -640,6 +640,25 @@ void ensureBuffers(oracle_sim& s) {
 }
 
 // ----------------------------------------------------- stepOnce (Integrator.cpp:312-797)
+// Refactorization by stamp and the bending RHS of the current pins (Integrator.cpp:341-372).
+void refreshFactor(oracle_sim& s) {
+  uint64_t now[4];
+  computeStamp(s, now);
+  const bool same = s.stampValid && now[0] == s.stampKey[0] && now[1] == s.stampKey[1] &&
+                    now[2] == s.stampKey[2] && now[3] == s.stampKey[3];
+  if (!same) {
+    const uint64_t structureNow = computeStructureStamp(s);
+    const bool re = !s.analyzed || structureNow != s.structureStamp;
+    analyzeAndFactorize(s, re);
+    s.structureStamp = structureNow;
+    std::memcpy(s.stampKey, now, sizeof(now));
+    s.stampValid = true;
+    assembleBendingRhs(s);
+  } else if (!s.bends.empty()) {
+    assembleBendingRhs(s);
+  }
+}
+
 int stepOnce(oracle_sim& s) {
   const oracle_config& cfg = s.cfg;
   const int n = s.n;
@@ -647,23 +666,7 @@ int stepOnce(oracle_sim& s) {
   const double invH = 1.0 / h;
   const double invH2 = 1.0 / (h * h);
   ensureBuffers(s);
-  {
-    uint64_t now[4];
-    computeStamp(s, now);
-    const bool same = s.stampValid && now[0] == s.stampKey[0] && now[1] == s.stampKey[1] &&
-                      now[2] == s.stampKey[2] && now[3] == s.stampKey[3];
-    if (!same) {
-      const uint64_t structureNow = computeStructureStamp(s);
-      const bool re = !s.analyzed || structureNow != s.structureStamp;
-      analyzeAndFactorize(s, re);
-      s.structureStamp = structureNow;
-      std::memcpy(s.stampKey, now, sizeof(now));
-      s.stampValid = true;
-      assembleBendingRhs(s);
-    } else if (!s.bends.empty()) {
-      assembleBendingRhs(s);
-    }
-  }
+  refreshFactor(s);
   if (!s.factorReady) return -1;
 
   const int threads = cfg.threads > 0 ? cfg.threads : g_threads();
@@ -1151,4 +1154,161 @@ extern "C" void oracle_project_one(const double* pa, const double* pb, double re
     return;
   }
   st(out, mul(d, rest / len));
+}
+
+// ------------------------------------------------------------ reference gradient (adjoint)
+// The differentiable substep: the reference's stepOnce with the iteration count fixed at
+// max_iterations (the gate is not differentiable) and an external force f entering the
+// prediction as x̂ = x + h·v + h²·g + h²·f/m. Serial FP64, summation in edge order.
+namespace {
+
+struct GradWork {
+  std::vector<double> xhat, b, col, w;
+};
+
+// One substep from (X, V) in place; iterates[k] (K+1 vectors of 3n) receives x^0..x^K if given.
+void forwardSubstep(oracle_sim& s, const double* force, std::vector<double>& X, std::vector<double>& V,
+                    std::vector<double>* iterates, GradWork& g) {
+  const int n = s.n, K = s.cfg.max_iterations;
+  const size_t dim = 3 * static_cast<size_t>(n);
+  const double h = s.cfg.dt, invH2 = 1.0 / (h * h), h2 = h * h;
+  const double damp = (1.0 - s.cfg.velocity_damping) * (1.0 / h);
+  g.xhat.assign(dim, 0.0);
+  g.b.assign(dim, 0.0);
+  g.col.assign(dim, 0.0);
+  g.w.assign(n, 0.0);
+  for (int v = 0; v < n; ++v)
+    for (int c = 0; c < 3; ++c) {
+      const size_t i = 3 * static_cast<size_t>(v) + c;
+      double xh = (X[i] + V[i] * h) + s.cfg.gravity[c] * h2;
+      if (force && s.m[v] > 0.0) xh += force[i] * (h2 / s.m[v]);
+      g.xhat[i] = xh;
+    }
+  std::vector<double> xk = X, xn = X;
+  if (iterates) std::copy(xk.begin(), xk.end(), iterates[0].begin());
+  for (int k = 0; k < K; ++k) {
+    for (int v = 0; v < n; ++v)
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = 3 * static_cast<size_t>(v) + c;
+        g.b[i] = s.m[v] * invH2 * g.xhat[i] + (s.bendRhs.empty() ? 0.0 : s.bendRhs[i]);
+      }
+    for (const Edge& e : s.edges) scatterEdge(s, e, projectEdge(xk.data(), e), g.b.data());
+    for (int v = 0; v < n; ++v)
+      if (s.pinned[v])
+        for (int c = 0; c < 3; ++c) g.b[3 * v + c] = s.q[3 * v + c];
+    for (int c = 0; c < 3; ++c) solveComponent(s, c, g.b.data(), g.col.data(), g.w.data());
+    xk = g.col;
+    if (iterates) std::copy(xk.begin(), xk.end(), iterates[k + 1].begin());
+  }
+  for (int v = 0; v < n; ++v)
+    for (int c = 0; c < 3; ++c) {
+      const size_t i = 3 * static_cast<size_t>(v) + c;
+      if (s.pinned[v]) {
+        V[i] = 0.0;
+        X[i] = s.q[i];
+      } else {
+        V[i] = (xk[i] - xn[i]) * damp;
+        X[i] = xk[i];
+      }
+    }
+}
+
+}  // namespace
+
+extern "C" int oracle_sim_gradient(oracle_sim* s, int substeps, const double* targets, const double* force,
+                                   double* loss, double* dkappa, double* dv0, double* dforce) {
+  ensureBuffers(*s);
+  refreshFactor(*s);
+  if (!s->factorReady || substeps < 0) return -1;
+  const int n = s->n, K = s->cfg.max_iterations, ne = static_cast<int>(s->edges.size());
+  const size_t dim = 3 * static_cast<size_t>(n);
+  const double h = s->cfg.dt, invH2 = 1.0 / (h * h), h2 = h * h;
+  const double damp = (1.0 - s->cfg.velocity_damping) * (1.0 / h);
+  GradWork g;
+  // forward with a checkpoint (x, v) at the start of every substep
+  std::vector<std::vector<double>> ckX(substeps), ckV(substeps);
+  std::vector<double> X = s->x, V = s->v;
+  for (int step = 0; step < substeps; ++step) {
+    ckX[step] = X;
+    ckV[step] = V;
+    forwardSubstep(*s, force, X, V, nullptr, g);
+  }
+  int nfree = 0;
+  for (int v = 0; v < n; ++v) nfree += s->pinned[v] ? 0 : 1;
+  double l = 0.0;
+  std::vector<double> xb(dim, 0.0), vb(dim, 0.0), fb(dim, 0.0), kb(ne, 0.0);
+  for (int v = 0; v < n; ++v) {
+    if (s->pinned[v]) continue;
+    for (int c = 0; c < 3; ++c) {
+      const size_t i = 3 * static_cast<size_t>(v) + c;
+      const double d = X[i] - targets[i];
+      l += d * d;
+      xb[i] = 2.0 * d / nfree;
+    }
+  }
+  if (loss) *loss = (nfree > 0) ? l / nfree : 0.0;
+  if (!dkappa && !dv0 && !dforce) return 0;
+  // reverse, substep by substep, recomputing each substep's iterates from its checkpoint
+  std::vector<std::vector<double>> it(K + 1, std::vector<double>(dim));
+  std::vector<double> xkb(dim), xnb(dim), xhb(dim), lam(dim), rhs(dim);
+  for (int step = substeps - 1; step >= 0; --step) {
+    X = ckX[step];
+    V = ckV[step];
+    forwardSubstep(*s, force, X, V, it.data(), g);  // g.xhat holds x̂ of this substep
+    for (int v = 0; v < n; ++v)
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = 3 * static_cast<size_t>(v) + c;
+        const bool p = s->pinned[v] != 0;
+        xkb[i] = p ? 0.0 : xb[i] + damp * vb[i];  // x' = x^K, v' = (x^K − x_n)·damp
+        xnb[i] = p ? 0.0 : -damp * vb[i];
+        xhb[i] = 0.0;
+      }
+    for (int k = K - 1; k >= 0; --k) {
+      for (size_t i = 0; i < dim; ++i) rhs[i] = xkb[i];  // pinned rows are zero
+      for (int c = 0; c < 3; ++c) solveComponent(*s, c, rhs.data(), lam.data(), g.w.data());
+      for (int v = 0; v < n; ++v) {
+        if (s->pinned[v]) continue;
+        for (int c = 0; c < 3; ++c) xhb[3 * v + c] += s->m[v] * invH2 * lam[3 * v + c];
+      }
+      std::fill(xkb.begin(), xkb.end(), 0.0);
+      const double* xk = it[k].data();
+      const double* xk1 = it[k + 1].data();
+      for (int e = 0; e < ne; ++e) {
+        const Edge& ed = s->edges[e];
+        const bool ap = s->pinned[ed.a] != 0, bp = s->pinned[ed.b] != 0;
+        if (ap && bp) continue;
+        const V3 la = ap ? V3{} : ld(&lam[3 * ed.a]), lb = bp ? V3{} : ld(&lam[3 * ed.b]);
+        const V3 le = sub(la, lb);
+        const V3 rel = sub(ld(xk + 3 * ed.a), ld(xk + 3 * ed.b));
+        const double len = length(rel);
+        V3 d{}, jl{};
+        if (len > kMinLength) {
+          d = mul(rel, ed.rest / len);
+          const V3 u = mul(rel, 1.0 / len);
+          jl = mul(sub(le, mul(u, dot(u, le))), ed.rest / len);  // ∂d/∂rel · λ_e (symmetric)
+        }
+        const V3 rel1 = sub(ld(xk1 + 3 * ed.a), ld(xk1 + 3 * ed.b));
+        kb[e] += dot(le, sub(d, rel1));
+        const V3 gk = mul(jl, ed.k);
+        if (!ap) st(&xkb[3 * ed.a], add(ld(&xkb[3 * ed.a]), gk));
+        if (!bp) st(&xkb[3 * ed.b], sub(ld(&xkb[3 * ed.b]), gk));
+      }
+    }
+    // x^0 = x_n; x̂ = x_n + h·v_n + h²·g + h²·f/m
+    for (int v = 0; v < n; ++v)
+      for (int c = 0; c < 3; ++c) {
+        const size_t i = 3 * static_cast<size_t>(v) + c;
+        if (s->pinned[v]) {
+          xb[i] = vb[i] = 0.0;
+          continue;
+        }
+        xb[i] = xnb[i] + xkb[i] + xhb[i];
+        vb[i] = h * xhb[i];
+        if (s->m[v] > 0.0) fb[i] += (h2 / s->m[v]) * xhb[i];
+      }
+  }
+  if (dkappa) std::copy(kb.begin(), kb.end(), dkappa);
+  if (dv0) std::copy(vb.begin(), vb.end(), dv0);
+  if (dforce) std::copy(fb.begin(), fb.end(), dforce);
+  return 0;
 }

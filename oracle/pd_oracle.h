@@ -132,6 +132,14 @@ int oracle_sim_coloring(oracle_sim* s, uint32_t* color_of, uint32_t* start, uint
 /* Bending constant RHS (assembleBendingRhs), 3n interleaved. */
 void oracle_sim_bend_rhs(oracle_sim* s, double* out);
 
+/* Loss L = mean over free vertices of |x − target|² after `substeps` substeps from the current
+ * state (which is left unchanged), with the iteration count fixed at max_iterations and an
+ * external per-vertex force f (3n, NULL = 0) entering the prediction as h²·f/m; and, by the
+ * adjoint method with per-substep checkpoints, its gradient w.r.t. the per-edge stiffness
+ * (n_edges), the initial velocities (3n) and f (3n). NULL outputs are skipped. Serial FP64. */
+int oracle_sim_gradient(oracle_sim* s, int substeps, const double* targets, const double* force,
+                        double* loss, double* dkappa, double* dv0, double* dforce);
+
 /* Closed-form projection of one edge (DistanceTerm::projectOne). */
 void oracle_project_one(const double* pa, const double* pb, double rest, double* out);
 

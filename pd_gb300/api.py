@@ -126,6 +126,8 @@ _SIGS = {
     "pd_sim_iteration_log": ([C.c_void_p, C.c_int32, _ip, _u8p, C.c_int32], C.c_int),
     "pd_sim_get_factor": ([C.c_void_p, C.c_int32, _ip, _ip, _ip, _dp, _dp, C.POINTER(C.c_int64)], C.c_int),
     "pd_sim_solve": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
+    "pd_sim_gradient": ([C.c_void_p, C.c_int32, C.POINTER(_dp), C.POINTER(_dp), _dp, C.POINTER(_dp),
+                         C.POINTER(_dp), C.POINTER(_dp)], C.c_int),
     "pd_scene_factor": ([C.POINTER(_Mesh), C.POINTER(_Cfg), _ip, _ip, _ip, _dp, _dp, C.POINTER(C.c_int64),
                          C.POINTER(_SimInfo)], C.c_int),
     "pd_scene_coloring": ([C.POINTER(_Mesh), C.POINTER(C.c_uint32), C.POINTER(C.c_int32)], C.c_int),
@@ -389,6 +391,40 @@ class Simulator:
         s = _SimStats()
         _check(self._lib.pd_sim_get_stats(self._h, i, C.byref(s)))
         return {f: getattr(s, f) for f, _ in _SimStats._fields_}
+
+    def gradient(self, substeps: int, targets, forces=None, grad=True):
+        """Loss and adjoint gradients of every instance (pd_sim_gradient): targets / forces are one
+        (n, 3) array per instance (or one array for a single cloth; forces may be None). Returns one
+        dict per instance with loss, dkappa (per edge), dv0 and dforce ((n, 3)), or a single dict."""
+        count = self.count
+        single = not isinstance(targets, (list, tuple))
+        tl = [targets] if single else list(targets)
+        fl = [forces] * count if (forces is None or single) else list(forces)
+        if single and forces is not None:
+            fl = [forces]
+        if len(tl) != count or len(fl) != count:
+            raise PdError(1, "one target (and force) array per instance")
+        keep = []
+        def arr(a):
+            a = np.ascontiguousarray(a, np.float64)
+            keep.append(a)
+            return _ptr(a, C.c_double)
+        tp = (_dp * count)(*[arr(t) for t in tl])
+        fp = (_dp * count)(*[(arr(f) if f is not None else _dp()) for f in fl])
+        loss = np.zeros(count)
+        outs = []
+        for i in range(count):
+            outs.append(dict(dkappa=np.zeros(self.n_edges[i]), dv0=np.zeros((self.n[i], 3)),
+                             dforce=np.zeros((self.n[i], 3))) if grad else {})
+        def ptrs(key):
+            if not grad:
+                return (_dp * count)()
+            return (_dp * count)(*[_ptr(o[key], C.c_double) for o in outs])
+        _check(self._lib.pd_sim_gradient(self._h, int(substeps), tp, fp, _ptr(loss, C.c_double), ptrs("dkappa"),
+                                         ptrs("dv0"), ptrs("dforce")))
+        for i, o in enumerate(outs):
+            o["loss"] = float(loss[i])
+        return outs[0] if single else outs
 
     def iteration_log(self, i: int = 0):
         it = np.zeros(self._last, np.int32)

@@ -26,6 +26,7 @@ UNITS = {
     "substep_mixed.cu": [],
     "substep_delta.cu": [],
     "substep_corr.cu": [],
+    "adjoint.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
 }
 

@@ -1196,6 +1196,97 @@ int pd_sim_solve(pd_sim* s, int32_t i, const double* b, double* x) {
   return PD_OK;
 }
 
+int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, const double* const* forces,
+                    double* loss, double* const* dkappa, double* const* dv0, double* const* dforce) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (substeps < 0) return fail(PD_ERR_INVALID_ARGUMENT, "substeps must be >= 0");
+  if (!targets) return fail(PD_ERR_INVALID_ARGUMENT, "null targets");
+  const int count = static_cast<int>(s->inst.size());
+  for (int i = 0; i < count; ++i)
+    if (!targets[i]) return fail(PD_ERR_INVALID_ARGUMENT, "null target of instance " + std::to_string(i));
+  if (const int rc_ = s->sync()) return rc_;
+  // device work arrays: per instance [target, force?, checkpoints, iterates, state and adjoints,
+  // per-edge terms, loss]
+  std::vector<size_t> off(count + 1, 0);
+  auto doublesOf = [&](int i) {
+    const Instance& I = s->inst[i];
+    const size_t n3 = 3 * static_cast<size_t>(I.scene.n), E = I.scene.edges.size();
+    const size_t K = static_cast<size_t>(std::max(0, I.cfg.max_iterations));
+    const size_t sub = static_cast<size_t>(std::max(1, substeps));
+    return n3 * (2 + 2 * sub + (K + 1) + 8) + 4 * E + 4;  // +4 keeps every instance 32-byte aligned
+  };
+  for (int i = 0; i < count; ++i) off[i + 1] = off[i] + (doublesOf(i) + 3) / 4 * 4;
+  double* dWork = nullptr;
+  pdg::GradDev* dG = nullptr;
+  PD_CUDA(cudaMalloc(&dWork, sizeof(double) * off[count]));
+  if (cudaMalloc(&dG, sizeof(pdg::GradDev) * count) != cudaSuccess) {
+    cudaFree(dWork);
+    return cudaFail(cudaGetLastError(), "gradient descriptors");
+  }
+  std::vector<pdg::GradDev> gd(count);
+  int smem = 0;
+  int rc = PD_OK;
+  for (int i = 0; i < count && rc == PD_OK; ++i) {
+    const Instance& I = s->inst[i];
+    const size_t n3 = 3 * static_cast<size_t>(I.scene.n), E = I.scene.edges.size();
+    const size_t K = static_cast<size_t>(std::max(0, I.cfg.max_iterations));
+    const size_t sub = static_cast<size_t>(std::max(1, substeps));
+    double* p = dWork + off[i];
+    pdg::GradDev& g = gd[i];
+    g.target = p;
+    p += n3;
+    g.force = (forces && forces[i]) ? p : nullptr;
+    p += n3;
+    g.ckX = p;
+    p += sub * n3;
+    g.ckV = p;
+    p += sub * n3;
+    g.it = p;
+    p += (K + 1) * n3;
+    double** vecs[] = {&g.xs, &g.vs, &g.xb, &g.vb, &g.xkb, &g.xnb, &g.xhb, &g.fb};
+    for (double** v : vecs) {
+      *v = p;
+      p += n3;
+    }
+    g.ge = p;
+    p += 3 * E;
+    g.kb = p;
+    p += E;
+    g.loss = p;
+    g.wantGrad = (dkappa && dkappa[i]) || (dv0 && dv0[i]) || (dforce && dforce[i]);
+    if (cudaMemcpyAsync(const_cast<double*>(g.target), targets[i], 8 * n3, cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess ||
+        (g.force && cudaMemcpyAsync(const_cast<double*>(g.force), forces[i], 8 * n3, cudaMemcpyHostToDevice,
+                                    s->stream) != cudaSuccess))
+      rc = cudaFail(cudaGetLastError(), "gradient inputs");
+    const int need = 48 * I.scene.n;
+    if (need <= kMaxSmem && need > smem) smem = need;
+  }
+  if (rc == PD_OK && cudaMemcpyAsync(dG, gd.data(), sizeof(pdg::GradDev) * count, cudaMemcpyHostToDevice,
+                                     s->stream) != cudaSuccess)
+    rc = cudaFail(cudaGetLastError(), "gradient descriptors");
+  if (rc == PD_OK) {
+    const int lrc = pdg::launchGradient(s->dDesc, dG, count, substeps, smem, s->stream);
+    if (lrc != 0) rc = cudaFail(static_cast<cudaError_t>(lrc), "gradient launch");
+  }
+  for (int i = 0; i < count && rc == PD_OK; ++i) {
+    const pdg::GradDev& g = gd[i];
+    const Instance& I = s->inst[i];
+    const size_t n3 = 3 * static_cast<size_t>(I.scene.n), E = I.scene.edges.size();
+    bool ok = !loss || cudaMemcpyAsync(loss + i, g.loss, 8, cudaMemcpyDeviceToHost, s->stream) == cudaSuccess;
+    if (g.wantGrad) {
+      if (dkappa && dkappa[i]) ok = ok && cudaMemcpyAsync(dkappa[i], g.kb, 8 * E, cudaMemcpyDeviceToHost, s->stream) == cudaSuccess;
+      if (dv0 && dv0[i]) ok = ok && cudaMemcpyAsync(dv0[i], g.vb, 8 * n3, cudaMemcpyDeviceToHost, s->stream) == cudaSuccess;
+      if (dforce && dforce[i]) ok = ok && cudaMemcpyAsync(dforce[i], g.fb, 8 * n3, cudaMemcpyDeviceToHost, s->stream) == cudaSuccess;
+    }
+    if (!ok) rc = cudaFail(cudaGetLastError(), "gradient results");
+  }
+  if (rc == PD_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = cudaFail(cudaGetLastError(), "gradient");
+  cudaFree(dG);
+  cudaFree(dWork);
+  return rc;
+}
+
 int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* perm, int32_t* colptr,
                     int32_t* rowidx, double* val, double* dinv, int64_t* nnz, pd_sim_info* info) {
   if (!mesh || !cfg) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");

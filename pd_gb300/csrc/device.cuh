@@ -155,6 +155,32 @@ int deltaResidentCtas(int smemBytes);
 int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
 constexpr int kDeltaThreads = 512;
 
+// Work arrays of one gradient problem (adjoint.cu): the loss is the mean over free vertices of
+// |x_S − target|² after S substeps with the iteration count fixed.
+struct GradDev {
+  const double* target;  // 3n
+  const double* force;   // 3n or null
+  double* ckX;           // S × 3n checkpoints of x
+  double* ckV;           // S × 3n checkpoints of v
+  double* it;            // (K + 1) × 3n iterates of the substep being reversed
+  double* xs;            // working state
+  double* vs;
+  double* xb;            // adjoints
+  double* vb;
+  double* xkb;
+  double* xnb;
+  double* xhb;
+  double* ge;            // 3E: κ_e·J_e·(λ_a − λ_b)
+  double* kb;            // E
+  double* fb;            // 3n
+  double* loss;          // 1
+  int32_t wantGrad;
+};
+// Loss (and, where wantGrad, gradients) of `count` problems, one CTA each (smemBytes: 48·n when
+// the solve vectors fit).
+int launchGradient(const InstanceDev* dInstances, const GradDev* dGrads, int count, int substeps, int smemBytes,
+                   void* stream);
+
 constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per
                                       // barrier beat more threads per level there)

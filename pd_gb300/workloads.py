@@ -16,6 +16,11 @@ library's ``pd_make_grid`` (the reference ``makeScene``), with the parameters be
                      shear on for half (κs = 0.4κ), bend for a quarter (κb = 0.02κ), pins drawn from
                      {two corners of the top row, the whole top row, one top corner}, h = 1/300,
                      10 iterations, 300 substeps.
+* ``differentiable`` 64×64, 1 m², corners of row 0 pinned, distance + shear edges, uniform mass
+                     1 kg, h = 1/300, 10 iterations with the gate off, no damping, 120 substeps.
+                     Returns the scene (every edge at κ = 2300), the config, the substep count and
+                     the hidden per-edge stiffness κ*_e = 2300·exp(N(0, 0.3²)) from a seed; the loss
+                     targets are the final positions of a run with κ*.
 Random draws use splitmix64 on integers, so every machine produces the same scenes.
 """
 from __future__ import annotations
@@ -101,3 +106,19 @@ def batch(count: int = 512, seed: int = 512, max_side: int = 128):
 
 WORKLOADS = {"cloth40_plain": cloth40_plain, "cloth40_full": cloth40_full, "cloth256": cloth256,
              "batch": batch}
+
+
+def _normal(rng: SplitMix64) -> float:
+    """Standard normal by Box–Muller from two splitmix64 uniforms."""
+    u1 = max(rng.uniform(), 1e-300)
+    u2 = rng.uniform()
+    return math.sqrt(-2.0 * math.log(u1)) * math.cos(2.0 * math.pi * u2)
+
+
+def differentiable(side: int = 64, substeps: int = 120, seed: int = 5):
+    cfg = _base(grid_nx=side, grid_ny=side, grid_spacing=1.0 / (side - 1), max_iterations=10,
+                shear_stiffness=2300.0, residual_tolerance=0.0, rel_tolerance=0.0, abs_tolerance=0.0)
+    scene = make_grid(cfg)
+    rng = SplitMix64(seed)
+    kstar = np.array([2300.0 * math.exp(0.3 * _normal(rng)) for _ in range(scene.edges.shape[0])])
+    return scene, cfg, substeps, kstar

@@ -276,3 +276,46 @@ def test_thread_count_independence(oracle):
         s.step(5)
         out.append(s.state()[0])
     assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+
+
+def _fd_problem(side=10, substeps=12, seed=3):
+    from pd_gb300 import workloads as W
+    from tests.helpers import oracle_twin
+    scene, cfg, S, kstar = W.differentiable(side=side, substeps=substeps)
+    twin = oracle_twin(scene, cfg)
+    twin.set_edge_stiffness(kstar)
+    twin.step(S)
+    targets = twin.state()[0]
+    rng = np.random.default_rng(seed)
+    force = rng.normal(0.0, 0.05, (scene.n, 3))
+    return scene, cfg, S, targets, force, rng
+
+
+def test_oracle_gradient_matches_central_differences():
+    """The CPU reference gradient (adjoint, FP64) against central differences of its own loss,
+    directions in stiffness, initial velocity and external force."""
+    from tests.helpers import oracle_twin
+    scene, cfg, S, targets, force, rng = _fd_problem()
+    orc = oracle_twin(scene, cfg)
+    g = orc.gradient(S, targets, force)
+    x0, v0 = orc.state()
+    k0 = np.asarray(scene.edge_stiffness, np.float64)
+
+    def loss(k, v, f):
+        o = oracle_twin(scene, cfg)
+        o.set_edge_stiffness(k)
+        o.set_state(x0, v)
+        return o.gradient(S, targets, f, grad=False)["loss"]
+
+    eps = 1e-4
+    for _ in range(3):
+        dk = k0 * rng.normal(0.0, 0.05, k0.shape)
+        dv = rng.normal(0.0, 0.1, v0.shape)
+        df = rng.normal(0.0, 0.05, force.shape)
+        fd = (loss(k0 + eps * dk, v0 + eps * dv, force + eps * df)
+              - loss(k0 - eps * dk, v0 - eps * dv, force - eps * df)) / (2 * eps)
+        adj = g["dkappa"] @ dk + np.sum(g["dv0"] * dv) + np.sum(g["dforce"] * df)
+        assert abs(fd - adj) <= 1e-6 * abs(adj), (fd, adj)
+    # the state is left unchanged and the loss-only call agrees
+    assert np.array_equal(orc.state()[0], x0)
+    assert orc.gradient(S, targets, force, grad=False)["loss"] == g["loss"]
