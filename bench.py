@@ -50,7 +50,11 @@ def kernel_name(info):
         return "substepMixedClusterKernel" if ctas > 1 else "substepMixedKernel"
     if kind == 3:
         return "substepDenseClusterKernel"
-    return "substepDeltaKernel"
+    if kind == 4:
+        return "substepDeltaKernel"
+    return "substepCorrKernel"
+
+
 UNIT = "substeps/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -58,7 +62,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=600)  # the workload's substep count, ≥ 0.2 s of clocks
+    p.add_argument("--steps", type=int, default=None)  # default: 600 substeps (3 gradient batches)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--workload", default="cloth40_full")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -68,7 +72,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-pos-err", action="store_true")
     p.add_argument("--no-fp64-gpu", action="store_true")
-    return p.parse_args()
+    p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
+    p.add_argument("--fd-directions", type=int, default=64)
+    a = p.parse_args()
+    if a.steps is None:
+        a.steps = 3 if a.workload == "differentiable" else 600
+    return a
 
 
 def dist_env():
@@ -216,7 +225,8 @@ def cpu_baseline(scenes, cfgs, substeps_total, max_seconds, threads=0):
     done = 0
     t_total = 0.0
     sims = [oracle_twin(s, c, threads=ncores) for s, c in zip(scenes, cfgs)]
-    sims[0].step(1)  # factorization happens in the first step; exclude it
+    for s in sims:
+        s.step(1)  # factorization happens in the first step; exclude it
     for k in range(substeps_total):
         t0 = time.perf_counter()
         for s in sims:
@@ -225,7 +235,7 @@ def cpu_baseline(scenes, cfgs, substeps_total, max_seconds, threads=0):
         done += 1
         if t_total > max_seconds:
             break
-    return {"value": done / t_total, "unit": UNIT, "cores": ncores, "kind": "port",
+    return {"value": len(sims) * done / t_total, "unit": UNIT, "cores": ncores, "kind": "port",
             "sample": f"{done} consecutive substeps of the workload ({len(sims)} cloth(s)) on the CPU oracle, "
                       f"{t_total:.1f} s, OpenMP {ncores} threads"}
 
@@ -246,7 +256,7 @@ def run_reference(args):
         for s in sims:
             s.step(1)
     dt = time.perf_counter() - t0
-    value = args.steps / dt
+    value = len(sims) * args.steps / dt  # aggregate (cloth-)substeps/s
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -281,8 +291,34 @@ def time_fp64_gpu(P, args, stream, flush, max_steps=10):
             ends[j].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / k
-    return {"value": 1e3 / ms, "unit": UNIT, "steps": k, "kernel": kernel_name(sim.info(0)),
+    return {"value": len(scenes) * 1e3 / ms, "unit": UNIT, "steps": k, "kernel": kernel_name(sim.info(0)),
             "ctas_per_cloth": sim.info(0)["cluster_ctas"]}
+
+
+def time_fp64_one_at_a_time(P, args, budget_s=120.0):
+    """Aggregate cloth-substeps/s of the batch run one cloth per launch through the plain FP64
+    path: every cloth gets its own simulator, one warm-up and one timed substep (CUDA events);
+    the per-cloth times are summed. Past `budget_s` of wall time the remaining cloths are
+    extrapolated from the mean of those timed."""
+    import torch
+    scenes, cfgs, _ = workload(args.workload, args.batch_count, "fp64")
+    times = []
+    wall = time.perf_counter()
+    for s, c in zip(scenes, cfgs):
+        sim = P.Simulator([s], [c])
+        sim.step(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        sim.step(1, sync=False)
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b) / 1e3)
+        del sim
+        if time.perf_counter() - wall > budget_s:
+            break
+    total = sum(times) * len(scenes) / len(times)
+    return {"value": len(scenes) / total, "unit": UNIT, "cloths_timed": len(times), "cloths": len(scenes),
+            "how": "one cloth per launch, plain FP64 path, per-cloth launch times summed"}
 
 
 def position_error(P, args, scenes, cfgs, substeps):
@@ -347,40 +383,46 @@ def run_ours(args):
     if world > 1:
         torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
     t_max = float(t_local.item())
-    value = world * args.steps / t_max
+    count = len(scenes)
+    value = world * count * args.steps / t_max  # aggregate (cloth-)substeps/s
 
-    # ---- e2e: through the C ABI, state copied from pinned host memory and read back every step
-    x0, v0 = sim.state(0)
-    host_x = torch.from_numpy(x0.copy()).pin_memory()
-    host_v = torch.from_numpy(v0.copy()).pin_memory()
-    hx, hv = host_x.numpy(), host_v.numpy()
-    n0 = scenes[0].n
-    h2d = d2h = 0
+    # ---- e2e: through the C ABI, every cloth's state copied from pinned host memory and read
+    # back every step
+    host = []
+    for i in range(count):
+        x0, v0 = sim.state(i)
+        host.append((torch.from_numpy(x0.copy()).pin_memory(), torch.from_numpy(v0.copy()).pin_memory()))
+    hosts = [(hx.numpy(), hv.numpy()) for hx, hv in host]
     sim.set_stream(None)
-    for _ in range(args.warmup):
-        sim.set_state(0, hx, hv)
+
+    def e2e_step():
+        for i, (hx, hv) in enumerate(hosts):
+            sim.set_state(i, hx, hv)           # H2D from pinned memory: positions + velocities
         sim.step(1, sync=False)
-        sim.state(0)
+        for i, (hx, hv) in enumerate(hosts):
+            sim.state(i, out_x=hx, out_v=hv)   # D2H into pinned memory (the first waits for the step)
+
+    for _ in range(args.warmup):
+        e2e_step()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        sim.set_state(0, hx, hv)           # H2D from pinned memory: positions + velocities
-        sim.step(1, sync=False)
-        sim.state(0, out_x=hx, out_v=hv)   # D2H into pinned memory (waits for the step)
+        e2e_step()
     barrier()
     e2e_s = time.perf_counter() - t0
-    h2d = d2h = 2 * 24 * n0
+    h2d = d2h = sum(2 * 24 * sc.n for sc in scenes)
     e_local = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
     if world > 1:
         torch.distributed.all_reduce(e_local, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world * args.steps / float(e_local.item())
+    e2e_value = world * count * args.steps / float(e_local.item())
 
     # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
     # error of this mode against the FP64 CPU oracle after the workload's full substep count
     fp64_line = pos_err = None
     if rank == 0:
         if not args.no_fp64_gpu:
-            fp64_line = time_fp64_gpu(P, args, stream, flush)
+            fp64_line = (time_fp64_one_at_a_time(P, args) if len(scenes) > 1
+                         else time_fp64_gpu(P, args, stream, flush))
         if not args.no_pos_err:
             pos_err = position_error(P, args, scenes, cfgs, sub)
 
@@ -416,6 +458,10 @@ def run_ours(args):
         if fp64_line is not None:
             fp64_line["ratio"] = value / fp64_line["value"]
             line["fp64_gpu"] = fp64_line
+            if len(scenes) > 1 and not args.no_fp64_gpu:
+                batched = time_fp64_gpu(P, args, stream, flush)
+                batched["ratio"] = value / batched["value"]
+                line["fp64_gpu_batched"] = batched
         if pos_err is not None:
             line["pos_err"] = pos_err
         if not args.no_cpu_baseline:
@@ -426,11 +472,143 @@ def run_ours(args):
     return 0
 
 
+# ------------------------------------------------------------------------- gradients (C5)
+def grad_problems(count):
+    """`count` differentiable problems on one 64×64 cloth: hidden stiffness κ* from seeds 1..count,
+    targets = final positions of an FP64 run with κ*; parameters at κ = 2300, v0 = 0, f = 0."""
+    import copy
+    import pd_gb300 as P
+    from pd_gb300 import workloads as W
+    scene, cfg, S, _ = W.differentiable()
+    cfg = copy.copy(cfg)
+    cfg.precision = PRECISIONS["fp64"][0]
+    kstars = [W.differentiable(seed=s + 1)[3] for s in range(count)]
+    ref = P.Simulator([scene] * count, [cfg] * count)
+    for i, k in enumerate(kstars):
+        ref.set_edge_stiffness(k, i)
+    ref.step(S)
+    targets = [ref.state(i)[0] for i in range(count)]
+    return scene, cfg, S, targets
+
+
+def run_gradients(args):
+    """Gradients/s of the adjoint on a batch of differentiable problems, with the checks: central
+    differences of the GPU loss on 64 random directions (ε = 1e-6 and 1e-4) and the FP64 CPU
+    reference gradient (oracle) on problem 0."""
+    import torch
+    import pd_gb300 as P
+    from tests.helpers import oracle_twin  # checker only
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    count = args.grad_batch
+    scene, cfg, S, targets = grad_problems(count)
+    zero = np.zeros((scene.n, 3))
+    sim = P.Simulator([scene] * count, [cfg] * count)
+    for _ in range(args.warmup):
+        sim.gradient(S, targets, [zero] * count)
+    sampler = ClockSampler(local)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        grads = sim.gradient(S, targets, [zero] * count)
+    dt = time.perf_counter() - t0
+    clocks = sampler.stop()
+    value = count * args.steps / dt
+    # central differences of the loss of problem 0 along random directions, one batched launch each
+    rng = np.random.default_rng(1)
+    k0 = np.asarray(scene.edge_stiffness, np.float64)
+    g0 = grads[0]
+    dirs = [(k0 * rng.normal(0.0, 0.05, k0.shape), rng.normal(0.0, 0.1, (scene.n, 3)), rng.normal(0.0, 0.05, (scene.n, 3)))
+            for _ in range(args.fd_directions)]
+    fd_err = {}
+    for eps in (1e-6, 1e-4):
+        fd_sim = P.Simulator([scene] * (2 * len(dirs)), [cfg] * (2 * len(dirs)))
+        forces = []
+        for j, (dk, dv, df) in enumerate(dirs):
+            for s, sign in enumerate((1.0, -1.0)):
+                i = 2 * j + s
+                fd_sim.set_edge_stiffness(k0 + sign * eps * dk, i)
+                fd_sim.set_state(i, scene.positions, sign * eps * dv)
+                forces.append(sign * eps * df)
+        losses = fd_sim.gradient(S, [targets[0]] * (2 * len(dirs)), forces, grad=False)
+        errs, errs_n = [], []
+        for j, (dk, dv, df) in enumerate(dirs):
+            fd = (losses[2 * j]["loss"] - losses[2 * j + 1]["loss"]) / (2 * eps)
+            adj = g0["dkappa"] @ dk + np.sum(g0["dv0"] * dv) + np.sum(g0["dforce"] * df)
+            # relative to the directional derivative, and to its scale ‖g‖·‖d‖ per parameter group
+            scale = (np.linalg.norm(g0["dkappa"]) * np.linalg.norm(dk) + np.linalg.norm(g0["dv0"]) * np.linalg.norm(dv)
+                     + np.linalg.norm(g0["dforce"]) * np.linalg.norm(df))
+            errs.append(abs(fd - adj) / max(abs(adj), 1e-300))
+            errs_n.append(abs(fd - adj) / max(scale, 1e-300))
+        fd_err[f"eps_{eps:g}"] = {"max_rel": float(max(errs)), "median_rel": float(np.median(errs)),
+                                  "max_rel_to_gradient_scale": float(max(errs_n))}
+        del fd_sim
+    # FP64 CPU reference gradient of problem 0
+    orc = oracle_twin(scene, cfg, perm=sim.factor(0)["perm"])
+    tc = time.perf_counter()
+    r = orc.gradient(S, targets[0], zero)
+    cpu_s = time.perf_counter() - tc
+    rel = {k: float(np.linalg.norm(g0[k] - r[k]) / max(np.linalg.norm(r[k]), 1e-300))
+           for k in ("dkappa", "dv0", "dforce")}
+    info = sim.info(0)
+    n3 = 3 * scene.n
+    line = {"metric": METRIC, "value": value, "unit": "grads/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "differentiable", "problems": count, "vertices": scene.n,
+                       "edges": int(scene.edges.shape[0]), "substeps": S, "iterations": cfg.max_iterations,
+                       "gradient_of": "mean squared distance of free vertices to targets w.r.t. per-edge stiffness, "
+                                      "initial velocities, external force", "kernel": "gradientKernel",
+                       "factor_nnz": info["factor_nnz"], "l2": "not flushed (each step is seconds long)"},
+            "gpu_launches": args.steps,
+            "e2e": {"value": value, "unit": "grads/s", "h2d_bytes_per_step": count * 2 * 8 * n3,
+                    "d2h_bytes_per_step": count * (8 * (2 * n3 + scene.edges.shape[0]) + 8)},
+            "grad_check": {"fd_directions": len(dirs), **fd_err, "vs_cpu_reference_rel": rel,
+                           "loss_problem0": g0["loss"], "loss_cpu_reference": r["loss"]},
+            "clocks": clocks,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "grads/s", "cores": 1, "kind": "port",
+                             "sample": "one gradient of problem 0 by the oracle's serial FP64 adjoint"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "differentiable":
+        if args.impl == "reference":
+            return run_reference_gradients(args)
+        return run_gradients(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
+
+
+def run_reference_gradients(args):
+    """The oracle's serial FP64 adjoint on problem 0, per gradient."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from tests.helpers import oracle_twin
+    scene, cfg, S, targets = grad_problems(1)
+    zero = np.zeros((scene.n, 3))
+    orc = oracle_twin(scene, cfg)
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.gradient(S, targets[0], zero)
+    dt = time.perf_counter() - t0
+    value = steps / dt
+    line = {"metric": METRIC, "value": value, "unit": "grads/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": 0, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "differentiable", "problems": 1, "vertices": scene.n, "substeps": S},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "grads/s", "cores": 1, "kind": "port",
+                             "sample": f"{steps} gradients of problem 0, oracle serial FP64 adjoint"},
+            "e2e": {"value": value, "unit": "grads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 if __name__ == "__main__":
