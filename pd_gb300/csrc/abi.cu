@@ -338,7 +338,10 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oInvL = A.add(I.F.invL);
   I.oInvLT = A.add(I.F.invLT);
   I.oT = A.zeros(24 * n);
-  I.oLvlG32 = A.add(pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads : pdg::kBlockThreads));
+  // FP32 solve: the correction kernel's teams are 256-thread CTAs, the other mixed kernels' 1024
+  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, teamCtas)
+                                   : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
+                                                                                : pdg::kBlockThreads));
   I.oLrv32 = A.add(I.F.rowval32);
   I.oLcv32 = A.add(I.F.colval32);
   I.oInvL32 = A.add(I.F.invL32);
@@ -521,7 +524,10 @@ struct pd_sim {
     corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
     if (p == PD_PRECISION_MIXED) {
-      if (!planDelta()) corr = true;
+      if (!planDelta()) {
+        corr = true;
+        teamCtas = planCorr();
+      }
       return;
     }
     int want = inst[0].cfg.cluster_ctas;
@@ -577,6 +583,21 @@ struct pd_sim {
     teamCtas = team;
     delta = true;
     return true;
+  }
+  // CTAs per cloth of the correction kernel: a cluster for a few large cloths (as for the FP64
+  // supernodal kernel), one CTA per cloth for batches and small cloths.
+  int planCorr() const {
+    int want = inst[0].cfg.cluster_ctas;
+    if (want <= 0) {
+      int minN = 1 << 30;
+      for (const auto& I : inst) minN = std::min(minN, I.scene.n);
+      const int count = static_cast<int>(inst.size());
+      want = minN < 4096 ? 1 : count <= 9 ? 16 : count <= 19 ? 8 : count <= 38 ? 4 : count <= 76 ? 2 : 1;
+    }
+    int cs = 1;
+    while (cs * 2 <= std::min(want, 16)) cs *= 2;
+    while (cs > 1 && pdg::corrClusterSupported(cs) != cs) cs /= 2;
+    return cs;
   }
   // Largest cloth solved with the explicit inverse: the configured limit, capped by the
   // kernel's shared memory (denseSmem(n) ≤ kMaxSmem).
@@ -640,7 +661,7 @@ struct pd_sim {
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       // the correction kernel keeps its solve vectors in shared memory up to 48 KB, so that a
       // batch still runs four CTAs per SM
-      const int cap = corr ? 48 * 1024 : kMaxSmem;
+      const int cap = corr ? (teamCtas > 1 ? 0 : 48 * 1024) : kMaxSmem;
       if ((delta || need <= cap) && need > smem) smem = need;
     }
     smemBytes = smem;
@@ -961,7 +982,10 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
   } else if (s->delta) {
     rc = pdg::launchSubstepDelta(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (s->corr) {
-    rc = pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes, s->stream);
+    rc = s->teamCtas > 1
+             ? pdg::launchSubstepCorrCluster(s->dDesc, count, s->teamCtas, substeps, s->stream)
+             : pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes,
+                                      s->stream);
   } else if (s->dense) {
     rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (mixedSolve(p)) {

@@ -51,14 +51,17 @@ struct CorrectionSums {
 
   // Edge incidences [e0, e1) of E (other vertex | pinned << 31, ℓ, κ as FP32 bits) and bend
   // incidences [s0, s1) of S (a, b, c | pinned << 31, (−k)·w_v bits); lane gl of G takes every
-  // G-th. X holds positions as (hi, lo) float4 pairs per vertex.
+  // G-th. X holds positions as (hi, lo) float4 pairs per vertex; with CG they are read from L2
+  // (other CTAs write them).
+  template <bool CG = false>
   __device__ __forceinline__ void accumulate(const InstanceDev& I, const int4* E, int e0, int e1, const int4* S,
                                              int s0, int s1, const float4* X, float4 vh, float4 vl, int gl, int G) {
+    auto X_ = [&](int i) { return CG ? __ldcg(X + i) : X[i]; };
     for (int q = e0 + gl; q < e1; q += G) {
       const int4 e = E[q];
       const int o = e.x & 0x7fffffff;
       const float rest = __int_as_float(e.y), kap = __int_as_float(e.z);
-      const float3 rel = diffHL(vh, vl, X[2 * o], X[2 * o + 1]);  // x_v − x_o
+      const float3 rel = diffHL(vh, vl, X_(2 * o), X_(2 * o + 1));  // x_v − x_o
       const float len = sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
       float dx = 0.f, dy = 0.f, dz = 0.f;
       if (!(len <= 1e-12f)) {
@@ -83,8 +86,8 @@ struct CorrectionSums {
       const int4 st = S[q];
       const int ia = st.x & 0x7fffffff, ib = st.y & 0x7fffffff, ic = st.z & 0x7fffffff;
       const float fac = __int_as_float(st.w);
-      float4 ah = X[2 * ia], al = X[2 * ia + 1], bh = X[2 * ib], bl = X[2 * ib + 1], ch = X[2 * ic],
-             cl = X[2 * ic + 1];
+      float4 ah = X_(2 * ia), al = X_(2 * ia + 1), bh = X_(2 * ib), bl = X_(2 * ib + 1), ch = X_(2 * ic),
+             cl = X_(2 * ic + 1);
       const float3 u = diffHL(ah, al, bh, bl), w = diffHL(ch, cl, bh, bl);
       f[0] = fmaf(fac, u.x + w.x, f[0]);
       f[1] = fmaf(fac, u.y + w.y, f[1]);

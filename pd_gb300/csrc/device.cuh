@@ -153,6 +153,10 @@ int deltaResidentCtas(int smemBytes);
 // MIXED substep for cloths above the explicit-inverse limit, one CTA per instance: x ← x +
 // L⁻¹·(b − Ã·x) with the FP32 supernodal solve (smemBytes: 24·n when the solve vectors fit).
 int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
+// The same by a thread-block cluster of `cs` 256-thread CTAs per instance (vectors in L2).
+int launchSubstepCorrCluster(const InstanceDev* dInstances, int count, int cs, int substeps, void* stream);
+// `cs` if a cluster of that many correction-kernel CTAs can run on this device, else 0.
+int corrClusterSupported(int cs);
 constexpr int kDeltaThreads = 512;
 
 // Work arrays of one gradient problem (adjoint.cu): the loss is the mean over free vertices of

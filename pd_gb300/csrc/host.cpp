@@ -402,7 +402,7 @@ int phaseLength(const Factor& f, int i, int ph) {
 }
 }  // namespace
 
-std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads) {
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas) {
   const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
   std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
   for (int l = 0; l < nlev; ++l)
@@ -424,8 +424,8 @@ std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads) {
         // the longest group's latency chain: an L2 round trip (~600 cycles) per four unrolled
         // trips of the row loop, ~8 cycles per dependent FMA, ~30 per shuffle step
         const double trips = std::ceil(static_cast<double>(lmax) / G);
-        const double issue = R * G / 32.0 * (3.0 * std::ceil(lavg / G) + 4.0 * lg + 6.0) / 4.0;
-        const double chain = std::ceil(R * G / static_cast<double>(ctaThreads)) *
+        const double issue = R * G / 32.0 * (3.0 * std::ceil(lavg / G) + 4.0 * lg + 6.0) / (4.0 * ctas);
+        const double chain = std::ceil(R * G / static_cast<double>(ctaThreads * ctas)) *
                              (600.0 * std::ceil(trips / 4.0) + 8.0 * trips + 30.0 * lg + 600.0);
         const double cost = std::max(issue, chain);
         if (cost < best) {

@@ -99,8 +99,8 @@ void buildSupernodal(Factor& f, const SupernodeTree& tree);
 // instruction occupies its SMSP's pipe for ~80 cycles whatever its active lanes, so narrow groups
 // waste fewer lanes while wide groups spread a level's few long rows over more SMSPs.
 std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas);
-// The same for an FP32 solve run by one CTA of `ctaThreads` threads, where latency dominates.
-std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads);
+// The same for an FP32 solve run by `ctas` CTAs of `ctaThreads` threads, where latency dominates.
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas = 1);
 // Fills the mixed-precision fields of a factorized Factor (needs the supernodal fields).
 void buildMixed(Factor& f, const ScalarMatrix& A);
 // Explicit inverse Ã⁻¹ in vertex order, FP32, rows padded to `ld` (a multiple of 32) entries:

@@ -1,57 +1,190 @@
-// substep_corr.cu — MIXED substeps of cloths above the explicit-inverse limit, one CTA per cloth.
+// substep_corr.cu — MIXED substeps of cloths above the explicit-inverse limit: the correction form
+// with the FP32 supernodal solve, by one CTA per cloth or by a thread-block cluster per cloth.
 //
 // Each PD iteration is taken in correction form, x^{k+1} = x^k + L⁻¹·(b(x^k) − Ã·x^k): the
 // correction r = b − Ã·x comes matrix-free from one FP32 pass over each vertex's incidences
 // (correction.cuh, which also yields the reference's residual of x^k for the gate), one FP32
-// supernodal solve (solve32.cuh) turns it into Δ, and positions — FP32 hi/lo pairs — take Δ by an
-// exact two-sum. The solve's FP32 rounding is relative to Δ, not to x, and the fixed point (r = 0)
-// is the reference's; the iteration loop has no FP64 instruction (FP64 is left for the
-// once-per-substep prediction and velocity update), and there is one solve per iteration.
+// supernodal solve turns it into Δ, and positions — FP32 hi/lo pairs — take Δ by an exact
+// two-sum. The solve's FP32 rounding is relative to Δ, not to x, and the fixed point (r = 0) is the
+// reference's; the iteration loop has no FP64 instruction (FP64 is left for the once-per-substep
+// prediction and velocity update), and there is one solve per iteration.
 //
-// One 256-thread CTA per cloth, four CTAs per SM, so a batch of cloths fills the GPU; the host
-// orders a batch's descriptors by cost so that the largest cloths start first.
-// Positions and x̂ (as pairs) live in the instance's arrays (L2); the solve's two FP32 vectors
-// sit in shared memory when they fit.
+// One 256-thread CTA per cloth (four per SM, so a batch fills the GPU; the host orders a batch's
+// descriptors by cost so that the largest cloths start first), or a cluster of up to 16 CTAs per
+// cloth for large single cloths: vertex, edge and row loops are strided over the cluster, phases
+// are separated by cluster barriers, data other CTAs write are read through L2, and reductions go
+// through distributed shared memory. Positions and x̂ (as pairs) and the solve's two vectors live
+// in the instance's arrays; a one-CTA cloth keeps the solve vectors in shared memory when they fit.
 #include "correction.cuh"
 #include "solve32.cuh"
+#include "substep_team.cuh"
 
 namespace pdg {
 namespace {
 
 constexpr int kLanesPerVertex = 8;  // lanes sharing one vertex's incidences
 
-__device__ __forceinline__ float warpMax(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
+// The FP32 supernodal solve of solve32.cuh with its rows strided over a team (one CTA or a
+// cluster): Y holds the right-hand side on entry and Δ on exit (elimination order).
+template <bool CLUSTER>
+struct TeamSolve32 {
+  template <int G, class Body>
+  static __device__ __forceinline__ void rows(const Team<CLUSTER>& tm, int cnt, Body&& body) {
+    const int lane = threadIdx.x & (G - 1);
+    const int groups = static_cast<int>(blockDim.x) / G;
+    const int gid = tm.rank * groups + static_cast<int>(threadIdx.x) / G;
+    const int stride = tm.size * groups;
+    for (int base = 0; base < cnt; base += stride) {  // uniform trip count keeps shuffles converged
+      const int idx = base + gid;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      body.accumulate(idx, lane, G, a0, a1, a2);
+      if (G > 1) {
+        a0 = groupSumF<G>(a0);
+        a1 = groupSumF<G>(a1);
+        a2 = groupSumF<G>(a2);
+      }
+      if (lane == 0) body.finish(idx, a0, a1, a2);
+    }
+  }
+  template <class Body>
+  static __device__ __forceinline__ void dispatch(const Team<CLUSTER>& tm, int g, int cnt, Body&& body) {
+    switch (g) {
+      case 1: rows<1>(tm, cnt, body); break;
+      case 2: rows<2>(tm, cnt, body); break;
+      case 4: rows<4>(tm, cnt, body); break;
+      case 8: rows<8>(tm, cnt, body); break;
+      case 16: rows<16>(tm, cnt, body); break;
+      default: rows<32>(tm, cnt, body); break;
+    }
+  }
+  struct FwdGather {  // t_i = y_i − Σ_{j < s0} L_ij·y_j
+    const InstanceDev& I; const Team<CLUSTER>& tm; const float* Y; float* T; int beg, cnt;
+    __device__ void accumulate(int idx, int lane, int G, float& a0, float& a1, float& a2) const {
+      if (idx >= cnt) return;
+      const int i = I.lvlRows[beg + idx];
+#pragma unroll 4
+      for (int p = I.Lrp[i] + lane; p < I.offEnd[i]; p += G) {
+        const int j = I.Lci[p];
+        const float lv = I.Lrv32[p];
+        a0 = fmaf(lv, tm.ld(Y + 3 * j), a0);
+        a1 = fmaf(lv, tm.ld(Y + 3 * j + 1), a1);
+        a2 = fmaf(lv, tm.ld(Y + 3 * j + 2), a2);
+      }
+    }
+    __device__ void finish(int idx, float a0, float a1, float a2) const {
+      if (idx >= cnt) return;
+      const int i = I.lvlRows[beg + idx];
+      T[3 * i] = tm.ld(Y + 3 * i) - a0;
+      T[3 * i + 1] = tm.ld(Y + 3 * i + 1) - a1;
+      T[3 * i + 2] = tm.ld(Y + 3 * i + 2) - a2;
+    }
+  };
+  struct FwdDense {  // y_i = Σ_{c ≤ r} (L_SS⁻¹)_{rc}·t_{s0+c}
+    const InstanceDev& I; const Team<CLUSTER>& tm; float* Y; const float* T; int beg, cnt;
+    __device__ void accumulate(int idx, int lane, int G, float& a0, float& a1, float& a2) const {
+      if (idx >= cnt) return;
+      const int i = I.lvlRows[beg + idx];
+      const int s = I.rowSn[i];
+      const int s0 = I.snStart[s];
+      const int r = i - s0;
+      const float* X = I.invL32 + I.snInvOff[s] + (int64_t)r * (r + 1) / 2;
+#pragma unroll 4
+      for (int c = lane; c <= r; c += G) {
+        const float xv = X[c];
+        const int j = s0 + c;
+        a0 = fmaf(xv, tm.ld(T + 3 * j), a0);
+        a1 = fmaf(xv, tm.ld(T + 3 * j + 1), a1);
+        a2 = fmaf(xv, tm.ld(T + 3 * j + 2), a2);
+      }
+    }
+    __device__ void finish(int idx, float a0, float a1, float a2) const {
+      if (idx >= cnt) return;
+      const int i = I.lvlRows[beg + idx];
+      Y[3 * i] = a0;
+      Y[3 * i + 1] = a1;
+      Y[3 * i + 2] = a2;
+    }
+  };
+  struct BwdGather {  // t_k = D⁻¹_k·y_k − Σ_{i ≥ s1} L_ik·x_i
+    const InstanceDev& I; const Team<CLUSTER>& tm; const float* Y; float* T; int beg, cnt;
+    __device__ void accumulate(int idx, int lane, int G, float& a0, float& a1, float& a2) const {
+      if (idx >= cnt) return;
+      const int k = I.lvlRows[beg + idx];
+#pragma unroll 4
+      for (int p = I.offBeg[k] + lane; p < I.Lcp[k + 1]; p += G) {
+        const int i = I.Lri[p];
+        const float lv = I.Lcv32[p];
+        a0 = fmaf(lv, tm.ld(Y + 3 * i), a0);
+        a1 = fmaf(lv, tm.ld(Y + 3 * i + 1), a1);
+        a2 = fmaf(lv, tm.ld(Y + 3 * i + 2), a2);
+      }
+    }
+    __device__ void finish(int idx, float a0, float a1, float a2) const {
+      if (idx >= cnt) return;
+      const int k = I.lvlRows[beg + idx];
+      const float di = I.dinv32[k];
+      T[3 * k] = fmaf(tm.ld(Y + 3 * k), di, -a0);
+      T[3 * k + 1] = fmaf(tm.ld(Y + 3 * k + 1), di, -a1);
+      T[3 * k + 2] = fmaf(tm.ld(Y + 3 * k + 2), di, -a2);
+    }
+  };
+  struct BwdDense {  // x_k = Σ_{c ≥ r} (L_SS⁻¹)_{cr}·t_{s0+c}
+    const InstanceDev& I; const Team<CLUSTER>& tm; float* Y; const float* T; int beg, cnt;
+    __device__ void accumulate(int idx, int lane, int G, float& a0, float& a1, float& a2) const {
+      if (idx >= cnt) return;
+      const int k = I.lvlRows[beg + idx];
+      const int s = I.rowSn[k];
+      const int s0 = I.snStart[s];
+      const int sz = I.snStart[s + 1] - s0;
+      const int r = k - s0;
+      const float* XT = I.invLT32 + I.snInvOff[s] + (int64_t)r * sz - (int64_t)r * (r - 1) / 2;
+#pragma unroll 4
+      for (int c = lane; c < sz - r; c += G) {
+        const float xv = XT[c];
+        const int j = k + c;
+        a0 = fmaf(xv, tm.ld(T + 3 * j), a0);
+        a1 = fmaf(xv, tm.ld(T + 3 * j + 1), a1);
+        a2 = fmaf(xv, tm.ld(T + 3 * j + 2), a2);
+      }
+    }
+    __device__ void finish(int idx, float a0, float a1, float a2) const {
+      if (idx >= cnt) return;
+      const int k = I.lvlRows[beg + idx];
+      Y[3 * k] = a0;
+      Y[3 * k + 1] = a1;
+      Y[3 * k + 2] = a2;
+    }
+  };
+  static __device__ void run(const InstanceDev& I, const Team<CLUSTER>& tm, float* Y, float* T) {
+    for (int l = 0; l < I.nlevS; ++l) {
+      const int beg = I.lvlRowPtr[l], cnt = I.lvlRowPtr[l + 1] - beg;
+      dispatch(tm, I.lvlG32[4 * l + 0], cnt, FwdGather{I, tm, Y, T, beg, cnt});
+      tm.sync();
+      dispatch(tm, I.lvlG32[4 * l + 1], cnt, FwdDense{I, tm, Y, T, beg, cnt});
+      tm.sync();
+    }
+    for (int l = I.nlevS - 1; l >= 0; --l) {
+      const int beg = I.lvlRowPtr[l], cnt = I.lvlRowPtr[l + 1] - beg;
+      dispatch(tm, I.lvlG32[4 * l + 2], cnt, BwdGather{I, tm, Y, T, beg, cnt});
+      tm.sync();
+      dispatch(tm, I.lvlG32[4 * l + 3], cnt, BwdDense{I, tm, Y, T, beg, cnt});
+      tm.sync();
+    }
+  }
+};
 
-// Max over the CTA of non-negative values (NaN-skipping); `red` holds one slot per warp.
-__device__ __forceinline__ float blockMaxF(float v, float* red) {
-  v = warpMax(v);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float m = 0.f;
-  for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
-  return m;
-}
-
-__global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const InstanceDev* __restrict__ insts,
-                                                                  int substeps, int smemBytes) {
-  extern __shared__ float sm[];
-  __shared__ float red[32];
-  const InstanceDev& I = insts[blockIdx.x];
+template <bool CLUSTER>
+__device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, int substeps, float* Y, float* T,
+                                double* red, double* slots) {
+  int parity = 0;
   const int n = I.n, n3 = 3 * n;
-  const bool inSmem = 24 * n <= smemBytes;  // Y, T: 3n floats each
-  float* Y = inSmem ? sm : I.y32;
-  float* T = inSmem ? sm + n3 : I.t32;
+  const int TID = tm.tid(), NT = tm.count();
   float4* X = reinterpret_cast<float4*>(I.xhl);     // vertex v: hi at X[2v], lo at X[2v + 1]
   float4* Xh = reinterpret_cast<float4*>(I.xhathl);  // x̂ the same way
   float* xf = I.xhl;
   float* xhf = I.xhathl;
 
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {
+  for (int v = TID; v < n; v += NT) {
     float4 h, l;
     split(I.x[3 * v], h.x, l.x);
     split(I.x[3 * v + 1], h.y, l.y);
@@ -60,25 +193,24 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
     X[2 * v] = h;
     X[2 * v + 1] = l;
   }
-  __syncthreads();
+  tm.sync();
 
-  const int gl = threadIdx.x & (kLanesPerVertex - 1), group = threadIdx.x / kLanesPerVertex;
-  const int ngroups = blockDim.x / kLanesPerVertex;
+  const int gl = TID & (kLanesPerVertex - 1), group = TID / kLanesPerVertex, ngroups = NT / kLanesPerVertex;
   for (int step = 0; step < substeps; ++step) {
     // predict (Integrator.cpp:447-472): x_n in FP64, x̂ as a pair
-    float sc = 0.f;
-    for (int t = threadIdx.x; t < n3; t += blockDim.x) {
+    double sc = 0.0;
+    for (int t = TID; t < n3; t += NT) {
       const int v = t / 3, c = t - 3 * v;
-      const double p = static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+      const double p = static_cast<double>(tm.ld(xf + 8 * v + c)) + static_cast<double>(tm.ld(xf + 8 * v + 4 + c));
       const double xh = (p + I.v[t] * I.h) + I.gh2[c];
       I.xn[t] = p;
       float hi, lo;
       split(xh, hi, lo);
       xhf[8 * v + c] = hi;
       xhf[8 * v + 4 + c] = lo;
-      sc = fmaxf(sc, static_cast<float>(fabs(xh - p)));
+      sc = fmax(sc, fabs(xh - p));
     }
-    const float scMax = blockMaxF(sc, red);
+    const double scMax = teamMax(tm, sc, red, slots, parity);
     const double scale = (scMax < I.gScaleHH) ? I.gScaleHH : scMax;
     int used = 0;
     bool conv = false;
@@ -92,10 +224,10 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
         const float4 vc = active ? __ldg(I.tVtx + v) : make_float4(0.f, 0.f, 1.f, 0.f);
         CorrectionSums cs;
         if (vc.z == 0.f) {
-          const float4 vh = X[2 * v], vl = X[2 * v + 1];
-          cs.accumulate(I, I.tEdge, I.rstart[v], I.rstart[v + 1], I.tBend, I.bstart[v], I.bstart[v + 1], X, vh, vl,
-                        gl, kLanesPerVertex);
-          if (gl == 0) cs.addMass(vh, vl, Xh[2 * v], Xh[2 * v + 1], vc.x);
+          const float4 vh = tm.ld(X + 2 * v), vl = tm.ld(X + 2 * v + 1);
+          cs.accumulate<CLUSTER>(I, I.tEdge, I.rstart[v], I.rstart[v + 1], I.tBend, I.bstart[v], I.bstart[v + 1], X,
+                                 vh, vl, gl, kLanesPerVertex);
+          if (gl == 0) cs.addMass(vh, vl, tm.ld(Xh + 2 * v), tm.ld(Xh + 2 * v + 1), vc.x);
         }
         cs.reduce<kLanesPerVertex>();
         if (active && gl == 0) {
@@ -110,7 +242,7 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
           Y[3 * e + 2] = r.z;
         }
       }
-      const float resMax = blockMaxF(res, red);
+      const double resMax = teamMax(tm, static_cast<double>(res), red, slots, parity);
       bool stop = k == I.maxIter;
       if (I.useResidual && k >= 1) {
         lastRes = resMax;
@@ -119,27 +251,27 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
         stop = stop || conv;
       }
       if (stop) break;
-      LocalSolve32::run(I, Y, T);  // Y ← Δ
+      TeamSolve32<CLUSTER>::run(I, tm, Y, T);  // Y ← Δ
       // x^{k+1} = x^k + Δ as pairs; pinned rows take q
-      float dmax = 0.f;
-      for (int t = threadIdx.x; t < n3; t += blockDim.x) {
+      double dmax = 0.0;
+      for (int t = TID; t < n3; t += NT) {
         const int v = t / 3, c = t - 3 * v;
-        float hi = xf[8 * v + c], lo = xf[8 * v + 4 + c];
+        float hi = tm.ld(xf + 8 * v + c), lo = tm.ld(xf + 8 * v + 4 + c);
         if (I.pinned[v]) {
           const float* qf = reinterpret_cast<const float*>(I.qhl);
           const float qh = __ldg(qf + 8 * v + c), ql = __ldg(qf + 8 * v + 4 + c);
-          dmax = fmaxf(dmax, fabsf((qh - hi) + (ql - lo)));
+          dmax = fmax(dmax, static_cast<double>(fabsf((qh - hi) + (ql - lo))));
           hi = qh;
           lo = ql;
         } else {
-          const float d = Y[3 * I.iperm[v] + c];
-          dmax = fmaxf(dmax, fabsf(d));
+          const float d = tm.ld(Y + 3 * I.iperm[v] + c);
+          dmax = fmax(dmax, static_cast<double>(fabsf(d)));
           addHL(hi, lo, d);
         }
         xf[8 * v + c] = hi;
         xf[8 * v + 4 + c] = lo;
       }
-      const float diff = blockMaxF(dmax, red);
+      const double diff = teamMax(tm, dmax, red, slots, parity);
       if (!I.useResidual) {
         const double rel = (scale > 0.0) ? diff / scale : diff;
         const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
@@ -150,7 +282,7 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
       }
     }
     // velocity, damping, pin resnap (Integrator.cpp:774-791)
-    for (int t = threadIdx.x; t < n3; t += blockDim.x) {
+    for (int t = TID; t < n3; t += NT) {
       const int v = t / 3, c = t - 3 * v;
       if (I.pinned[v]) {
         I.v[t] = 0.0;
@@ -160,11 +292,11 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
           xf[8 * v + 4 + c] = __ldg(qf + 8 * v + 4 + c);
         }
       } else {
-        const double x = static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+        const double x = static_cast<double>(tm.ld(xf + 8 * v + c)) + static_cast<double>(tm.ld(xf + 8 * v + 4 + c));
         I.v[t] = (x - I.xn[t]) * I.dampInvH;
       }
     }
-    if (threadIdx.x == 0) {
+    if (TID == 0) {
       if (I.iterLog) I.iterLog[step] = used;
       if (I.convLog) I.convLog[step] = conv ? 1 : 0;
       *I.lastResidual = lastRes;
@@ -172,12 +304,52 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
       *I.converged = conv ? 1 : 0;
       if (conv) *I.earlyExits += 1;
     }
-    __syncthreads();
+    tm.sync();
   }
-  for (int t = threadIdx.x; t < n3; t += blockDim.x) {
+  for (int t = TID; t < n3; t += NT) {
     const int v = t / 3, c = t - 3 * v;
-    I.x[t] = I.pinned[v] ? I.q[t] : static_cast<double>(xf[8 * v + c]) + static_cast<double>(xf[8 * v + 4 + c]);
+    I.x[t] = I.pinned[v] ? I.q[t]
+                         : static_cast<double>(tm.ld(xf + 8 * v + c)) + static_cast<double>(tm.ld(xf + 8 * v + 4 + c));
   }
+}
+
+__global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const InstanceDev* __restrict__ insts,
+                                                                     int substeps, int smemBytes) {
+  extern __shared__ float sm[];
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  const InstanceDev& I = insts[blockIdx.x];
+  const bool inSmem = 24 * I.n <= smemBytes;  // Y, T: 3n floats each
+  float* Y = inSmem ? sm : I.y32;
+  float* T = inSmem ? sm + 3 * I.n : I.t32;
+  const Team<false> tm{0, 1};
+  runSubstepsCorr<false>(I, tm, substeps, Y, T, red, slots);
+}
+
+__global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const InstanceDev* __restrict__ insts,
+                                                                         int substeps) {
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+  const int cs = static_cast<int>(cl.num_blocks());
+  const InstanceDev& I = insts[blockIdx.x / cs];
+  const Team<true> tm{static_cast<int>(cl.block_rank()), cs};
+  runSubstepsCorr<true>(I, tm, substeps, I.y32, I.t32, red, slots);
+}
+
+cudaLaunchConfig_t corrClusterConfig(int blocks, int cs, void* stream, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
 }
 
 }  // namespace
@@ -191,6 +363,26 @@ int launchSubstepCorr(const InstanceDev* d, int count, int substeps, int smemByt
   }
   substepCorrKernel<<<count, kBlockThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
+}
+
+int corrClusterSupported(int cs) {
+  if (cs < 2 || cs > 16) return 0;
+  if (cs > 8) cudaFuncSetAttribute(substepCorrClusterKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = corrClusterConfig(cs, cs, nullptr, attr);
+  int clusters = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, substepCorrClusterKernel, &cfg);
+  if (e != cudaSuccess) cudaGetLastError();
+  return (e == cudaSuccess && clusters > 0) ? cs : 0;
+}
+
+int launchSubstepCorrCluster(const InstanceDev* d, int count, int cs, int substeps, void* stream) {
+  if (count <= 0 || substeps <= 0) return 0;
+  if (corrClusterSupported(cs) != cs) return static_cast<int>(cudaErrorInvalidConfiguration);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = corrClusterConfig(count * cs, cs, stream, attr);
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepCorrClusterKernel, d, substeps);
+  return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 
 }  // namespace pdg
