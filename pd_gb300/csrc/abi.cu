@@ -96,6 +96,7 @@ struct Instance {
       oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl, oXhl,
       oXhatHl;
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
+  int corrTeam = 1;     // correction kernel: CTAs (a cluster when > 1) running this instance
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
   int teamECap = 0, teamBCap = 0;
   size_t bytes = 0;
@@ -339,7 +340,7 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oInvLT = A.add(I.F.invLT);
   I.oT = A.zeros(24 * n);
   // FP32 solve: the correction kernel's teams are 256-thread CTAs, the other mixed kernels' 1024
-  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, teamCtas)
+  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam)
                                    : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
                                                                                 : pdg::kBlockThreads));
   I.oLrv32 = A.add(I.F.rowval32);
@@ -477,6 +478,8 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
 }
 
 constexpr int kMaxSmem = 200 * 1024;
+constexpr int kBatchCluster = 4;                // CTAs per large cloth of a MIXED batch
+constexpr int kBatchClusterMinVertices = 8192;  // "large"
 
 // Status code of a preparation failure message.
 int prepareCode(const std::string& err) {
@@ -504,8 +507,16 @@ struct pd_sim {
   bool dense = false;  // mixed modes: the cluster applies the explicit FP32 inverse
   bool delta = false;  // MIXED: a team of co-resident CTAs per cloth, correction-form dense solve
   bool corr = false;   // MIXED above the dense limit: one CTA per cloth, correction-form FP32 solve
+  int corrBig = 0;     // batch: instances (first in dDescOrder) run by clusters of kBatchCluster CTAs
+  cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
+  cudaEvent_t forkEv = nullptr, joinEv = nullptr;
 
-  ~pd_sim() { release(); }
+  ~pd_sim() {
+    release();
+    if (aux) cudaStreamDestroy(aux);
+    if (forkEv) cudaEventDestroy(forkEv);
+    if (joinEv) cudaEventDestroy(joinEv);
+  }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
 
   // CTAs per cloth for the supernodal FP64 kernel: the requested count, or 16 for up to nine
@@ -523,10 +534,27 @@ struct pd_sim {
     delta = false;
     corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
+    for (auto& I : inst) I.corrTeam = 1;
+    corrBig = 0;
     if (p == PD_PRECISION_MIXED) {
       if (!planDelta()) {
         corr = true;
         teamCtas = planCorr();
+        if (teamCtas > 1) {
+          for (auto& I : inst) I.corrTeam = teamCtas;
+        } else if (inst.size() > 1 && pdg::corrClusterSupported(kBatchCluster) == kBatchCluster) {
+          // a batch: the large cloths, whose one-CTA time would set the launch's makespan, get a
+          // small cluster each and run on a second stream beside the others
+          for (auto& I : inst)
+            if (I.scene.n >= kBatchClusterMinVertices) {
+              I.corrTeam = kBatchCluster;
+              ++corrBig;
+            }
+          if (corrBig == static_cast<int>(inst.size())) {  // all large: one clustered launch
+            teamCtas = kBatchCluster;
+            corrBig = 0;
+          }
+        }
       }
       return;
     }
@@ -661,7 +689,7 @@ struct pd_sim {
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       // the correction kernel keeps its solve vectors in shared memory up to 48 KB, so that a
       // batch still runs four CTAs per SM
-      const int cap = corr ? (teamCtas > 1 ? 0 : 48 * 1024) : kMaxSmem;
+      const int cap = corr ? ((teamCtas > 1 || inst[i].corrTeam > 1) ? 0 : 48 * 1024) : kMaxSmem;
       if ((delta || need <= cap) && need > smem) smem = need;
     }
     smemBytes = smem;
@@ -674,7 +702,10 @@ struct pd_sim {
         const Instance& I = inst[i];
         return static_cast<double>(I.F.colval.size()) + 8.0 * I.scene.edges.size() + 4.0 * I.scene.n;
       };
-      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost(a) > cost(b); });
+      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        if (inst[a].corrTeam != inst[b].corrTeam) return inst[a].corrTeam > inst[b].corrTeam;  // clustered first
+        return cost(a) > cost(b);
+      });
       std::vector<pdg::InstanceDev> sorted;
       for (size_t i : order) sorted.push_back(desc[i]);
       if (!dDescOrder) PD_CUDA(cudaMalloc(&dDescOrder, sizeof(pdg::InstanceDev) * inst.size()));
@@ -982,10 +1013,28 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
   } else if (s->delta) {
     rc = pdg::launchSubstepDelta(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (s->corr) {
-    rc = s->teamCtas > 1
-             ? pdg::launchSubstepCorrCluster(s->dDesc, count, s->teamCtas, substeps, s->stream)
-             : pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes,
-                                      s->stream);
+    if (s->teamCtas > 1) {
+      rc = pdg::launchSubstepCorrCluster(s->dDesc, count, s->teamCtas, substeps, s->stream);
+    } else if (s->corrBig > 0) {  // large cloths in clusters on the second stream, the rest here
+      if (!s->aux) {
+        PD_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+        PD_CUDA(cudaEventCreateWithFlags(&s->forkEv, cudaEventDisableTiming));
+        PD_CUDA(cudaEventCreateWithFlags(&s->joinEv, cudaEventDisableTiming));
+      }
+      PD_CUDA(cudaEventRecord(s->forkEv, s->stream));
+      PD_CUDA(cudaStreamWaitEvent(s->aux, s->forkEv, 0));
+      rc = pdg::launchSubstepCorrCluster(s->dDescOrder, s->corrBig, kBatchCluster, substeps, s->aux);
+      if (rc == 0)
+        rc = pdg::launchSubstepCorr(s->dDescOrder + s->corrBig, count - s->corrBig, substeps, s->smemBytes,
+                                    s->stream);
+      if (rc == 0) {
+        PD_CUDA(cudaEventRecord(s->joinEv, s->aux));
+        PD_CUDA(cudaStreamWaitEvent(s->stream, s->joinEv, 0));
+      }
+    } else {
+      rc = pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes,
+                                  s->stream);
+    }
   } else if (s->dense) {
     rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
   } else if (mixedSolve(p)) {

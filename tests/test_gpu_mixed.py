@@ -197,3 +197,24 @@ def test_correction_gates_and_pins(pdg, strategy):
         assert max_rel(sim.state()[0], orc.state()[0]) < TOL_POS
         it_g, cv_g = sim.iteration_log()
         assert np.mean(it_g == it_o[-len(it_g):]) > 0.95
+
+
+def test_batch_with_large_cloths_on_clusters(pdg):
+    """A MIXED batch whose large cloths run as 4-CTA clusters on a second stream while the small
+    ones run one CTA each: every cloth still matches the oracle."""
+    sides = [(92, 92), (20, 24), (96, 90), (16, 40), (30, 30)]
+    scenes, cfgs = [], []
+    for nx, ny in sides:
+        cfg = with_mode(W._base(grid_nx=nx, grid_ny=ny, grid_spacing=1.0 / (max(nx, ny) - 1), max_iterations=10,
+                                shear_stiffness=900.0), "mixed")
+        scenes.append(pdg.make_grid(cfg))
+        cfgs.append(cfg)
+    sim = pdg.Simulator(scenes, cfgs)
+    assert sim.info(0)["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
+    for _ in range(2):
+        sim.step(10)
+    sim.synchronize()
+    for i, (s, c) in enumerate(zip(scenes, cfgs)):
+        orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
+        orc.step(20)
+        assert max_rel(sim.state(i)[0], orc.state()[0]) < TOL_POS, i
