@@ -137,7 +137,8 @@ std::string prepare(Instance& I, bool reanalyze) {
 
 // Shared memory of the team kernel for one instance: positions as hi/lo pairs (32 B a vertex),
 // the padded correction (12 B a row), `resRows` rows of Ã⁻¹, and per owned vertex x, x_n, x̂, v
-// (FP64) and Δ (FP32). Fills *resRows with as many rows as fit in kDeltaSmem (even unless all).
+// (FP64) and Δ (FP32). Fills *resRows with as many rows as fit in kDeltaSmem (a multiple of four
+// unless all).
 constexpr int kDeltaSmem = 220 * 1024;
 // Pin positions as FP32 pairs per vertex: hi (x, y, z, 0), lo (x, y, z, 0) with hi = fl32(q) and
 // lo = fl32(q − hi), the split the team kernel applies to positions.
@@ -170,13 +171,14 @@ int deltaSmem(const Instance& I, int team, int* resRows) {
   int eCap = 0, bCap = 0;
   teamCaps(I, team, &eCap, &bCap);
   // positions, correction, incidences, vertex constants, FP64 state, Δ, incidence offsets
-  // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 48·chunk partial sums of Δ)
-  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 144L * chunk + 8L * (chunk + 1);
+  // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 24·chunk partial sums of Δ over
+  // up to two column segments)
+  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 120L * chunk + 8L * (chunk + 1);
   long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (4L * ld) : 0;
   if (rows >= chunk) {
     rows = chunk;
   } else {
-    rows &= ~1L;
+    rows &= ~3L;  // whole groups of four rows
   }
   *resRows = static_cast<int>(rows);
   return static_cast<int>(fixed + 4L * rows * ld);

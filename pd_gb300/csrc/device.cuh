@@ -97,7 +97,7 @@ struct InstanceDev {
   const double* Vval;
   // correction-form dense solve by a team of CTAs (MIXED). Exchange words carry
   // (epoch << 32 | FP32 bits): a reader knows a word is current from its epoch alone.
-  int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (even unless all)
+  int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (multiple of 4 unless all)
   int32_t teamECap, teamBCap;  // most edge / bend incidences of one CTA's vertices
   const int4* tEdge;           // per edge incidence (rstart order): other | pinned << 31, rest, κ (FP32 bits), 0
   const int4* tBend;           // per bend incidence (bstart order): a, b, c (| pinned << 31), (−k)·w_v bits

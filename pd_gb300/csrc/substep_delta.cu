@@ -45,7 +45,8 @@ constexpr int kWarps = kDeltaThreads / 32;
 constexpr int kGroup = 16;                  // lanes per vertex in the correction pass
 constexpr long long kSpinLimit = 1ll << 22; // poll rounds before an exchange gives up
 constexpr int kMaxTeam = 256;               // partials one polling warp covers (kMaxTeam / 32 a lane)
-constexpr int kSegments = 4;                // most column segments a row pair of Ã⁻¹ is split into
+constexpr int kSegments = 2;                // most column segments a row group of Ã⁻¹ is split into
+constexpr int kGroupRows = 2;               // rows of Ã⁻¹ one warp applies together
 constexpr int kPartStride = 16;             // words between two CTAs' partials: one L2 line each
 
 __device__ __forceinline__ unsigned long long loadRelaxed(const unsigned long long* p) {
@@ -154,46 +155,44 @@ __device__ __forceinline__ double warpMaxD(double v) {
   return v;
 }
 
-// Rows of Ã⁻¹ times the three components of R over the float4 columns [jb, je), two rows per
-// warp; A rows from shared or global memory. Sums of the pair land in dl[3·li + c].
-template <bool SMEM>
-__device__ __forceinline__ void rowPair(const float* A0, const float* A1, bool two, const float* Rs, int ld, int li,
-                                        int jb, int je, float* dl) {
+// Up to NR rows of Ã⁻¹ (starting at A0, nr of them) times the three components of R over the
+// float4 columns [jb, je), one warp; each R load serves NR rows. A rows from shared or global
+// memory. Sums land in dl[3·(li + r) + c].
+template <int NR, bool SMEM>
+__device__ __forceinline__ void rowGroup(const float* A0, int nr, const float* Rs, int ld, int li, int jb, int je,
+                                         float* dl) {
   const int lane = threadIdx.x & 31;
-  const float4* a0 = reinterpret_cast<const float4*>(A0);
-  const float4* a1 = reinterpret_cast<const float4*>(A1);
+  const float4* a = reinterpret_cast<const float4*>(A0);
+  const int ld4 = ld / 4;
   const float4* rx = reinterpret_cast<const float4*>(Rs);
   const float4* ry = reinterpret_cast<const float4*>(Rs + ld);
   const float4* rz = reinterpret_cast<const float4*>(Rs + 2 * ld);
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
+  float s[NR][3];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) s[r][0] = s[r][1] = s[r][2] = 0.f;
 #pragma unroll 4
   for (int j = jb + lane; j < je; j += 32) {
     const float4 x = rx[j], y = ry[j], z = rz[j];
-    const float4 u = SMEM ? a0[j] : __ldg(a0 + j);
-    const float4 w = SMEM ? a1[j] : __ldg(a1 + j);
-    s0 = fmaf(u.x, x.x, fmaf(u.y, x.y, fmaf(u.z, x.z, fmaf(u.w, x.w, s0))));
-    s1 = fmaf(u.x, y.x, fmaf(u.y, y.y, fmaf(u.z, y.z, fmaf(u.w, y.w, s1))));
-    s2 = fmaf(u.x, z.x, fmaf(u.y, z.y, fmaf(u.z, z.z, fmaf(u.w, z.w, s2))));
-    t0 = fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, fmaf(w.w, x.w, t0))));
-    t1 = fmaf(w.x, y.x, fmaf(w.y, y.y, fmaf(w.z, y.z, fmaf(w.w, y.w, t1))));
-    t2 = fmaf(w.x, z.x, fmaf(w.y, z.y, fmaf(w.z, z.z, fmaf(w.w, z.w, t2))));
-  }
-  s0 = groupSum<32>(s0);
-  s1 = groupSum<32>(s1);
-  s2 = groupSum<32>(s2);
-  t0 = groupSum<32>(t0);
-  t1 = groupSum<32>(t1);
-  t2 = groupSum<32>(t2);
-  if (lane == 0) {
-    dl[3 * li] = s0;
-    dl[3 * li + 1] = s1;
-    dl[3 * li + 2] = s2;
-    if (two) {
-      dl[3 * li + 3] = t0;
-      dl[3 * li + 4] = t1;
-      dl[3 * li + 5] = t2;
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      if (r < nr) {
+        const float4 u = SMEM ? a[r * ld4 + j] : __ldg(a + r * ld4 + j);
+        s[r][0] = fmaf(u.x, x.x, fmaf(u.y, x.y, fmaf(u.z, x.z, fmaf(u.w, x.w, s[r][0]))));
+        s[r][1] = fmaf(u.x, y.x, fmaf(u.y, y.y, fmaf(u.z, y.z, fmaf(u.w, y.w, s[r][1]))));
+        s[r][2] = fmaf(u.x, z.x, fmaf(u.y, z.y, fmaf(u.z, z.z, fmaf(u.w, z.w, s[r][2]))));
+      }
     }
   }
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s[r][c] = groupSum<32>(s[r][c]);
+  if (lane == 0)
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+      if (r < nr)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dl[3 * (li + r) + c] = s[r][c];
 }
 
 __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const InstanceDev* __restrict__ insts,
@@ -260,8 +259,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   unsigned long long* ptagB = I.ptag + 2 * kPartStride * team;
   const int wlo = I.window[2 * rank], whi = I.window[2 * rank + 1];
   // GEMV work: row pairs × column segments over the warps
-  const int pairs = (m + 1) / 2;
-  const int segs = pairs > 0 ? max(1, min(kSegments, kWarps / pairs)) : 1;
+  const int groups = (m + kGroupRows - 1) / kGroupRows;
+  const int segs = groups > 0 ? max(1, min(kSegments, kWarps / groups)) : 1;
   const int q4 = ld / 4;
   __syncthreads();
 
@@ -354,18 +353,16 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         break;
       }
 
-      // this CTA's rows of Ã⁻¹·r: row pairs × column segments over the warps
-      for (int task = warp; task < pairs * segs; task += kWarps) {
-        const int li = 2 * (task / segs), sg = task - (task / segs) * segs;
+      // this CTA's rows of Ã⁻¹·r: groups of kGroupRows rows × column segments over the warps
+      for (int task = warp; task < groups * segs; task += kWarps) {
+        const int li = kGroupRows * (task / segs), sg = task - (task / segs) * segs;
         const int jb = q4 * sg / segs, je = q4 * (sg + 1) / segs;
-        const bool two = li + 1 < m;
+        const int nr = min(kGroupRows, m - li);
         float* out = dl + sg * 3 * chunk;
-        if (li < resRows) {  // resRows is even unless it covers every row: the pair is resident
-          const float* A0 = As + static_cast<size_t>(li) * ld;
-          rowPair<true>(A0, two ? A0 + ld : A0, two, Rs, ld, li, jb, je, out);
+        if (li < resRows) {  // resRows is a multiple of 4 unless it covers every row
+          rowGroup<kGroupRows, true>(As + static_cast<size_t>(li) * ld, nr, Rs, ld, li, jb, je, out);
         } else {
-          const float* A0 = I.Ainv + static_cast<size_t>(rb + li) * ld;
-          rowPair<false>(A0, two ? A0 + ld : A0, two, Rs, ld, li, jb, je, out);
+          rowGroup<kGroupRows, false>(I.Ainv + static_cast<size_t>(rb + li) * ld, nr, Rs, ld, li, jb, je, out);
         }
       }
       __syncthreads();
