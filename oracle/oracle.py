@@ -34,6 +34,11 @@ class _Config(C.Structure):
         ("abs_tolerance", C.c_double),
         ("residual_tolerance", C.c_double),
         ("threads", C.c_int),
+        ("cheb_mode", C.c_int),
+        ("cheb_rho", C.c_double),
+        ("cheb_start", C.c_int),
+        ("cheb_m", C.c_double),
+        ("cheb_d", C.c_double),
     ]
 
 
@@ -120,6 +125,11 @@ class Config:
     abs_tolerance: float = 1.0e-12
     residual_tolerance: float = 1.0e-3
     threads: int = 0
+    cheb_mode: int = 0        # 0 off, 1 ρ recurrence (PD_CHEB=1), 2 roots over [m−δ, m+δ] (interval)
+    cheb_rho: float = 0.98
+    cheb_start: int = 10
+    cheb_m: float = 1.0
+    cheb_d: float = 1.0
 
     def c(self):
         c = _Config()
@@ -132,6 +142,11 @@ class Config:
         c.abs_tolerance = self.abs_tolerance
         c.residual_tolerance = self.residual_tolerance
         c.threads = self.threads
+        c.cheb_mode = self.cheb_mode
+        c.cheb_rho = self.cheb_rho
+        c.cheb_start = self.cheb_start
+        c.cheb_m = self.cheb_m
+        c.cheb_d = self.cheb_d
         return c
 
 

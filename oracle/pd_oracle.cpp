@@ -659,6 +659,25 @@ void refreshFactor(oracle_sim& s) {
   }
 }
 
+// Whether iteration k blends, and its weight ω_k from ω_{k−1} (Integrator.cpp:590-617): mode 1
+// ω = 2/(2−ρ²) at k = S+1, then 4/(4−ρ²ω); mode 2 ω_k = 1/(m + δ·cos(π(2j−1)/(2T))), j = k+1,
+// T = the iteration budget, from k = 0.
+bool chebBlends(const oracle_config& cfg, int k) {
+  return cfg.cheb_mode == 2 || (cfg.cheb_mode == 1 && k > cfg.cheb_start);
+}
+
+double chebOmega(const oracle_config& cfg, int k, double prev) {
+  if (cfg.cheb_mode == 1) {
+    if (k == cfg.cheb_start + 1) return 2.0 / (2.0 - cfg.cheb_rho * cfg.cheb_rho);
+    return 4.0 / (4.0 - cfg.cheb_rho * cfg.cheb_rho * prev);
+  }
+  const double pi = 3.14159265358979323846;
+  const double T = static_cast<double>(cfg.max_iterations);
+  const double j = static_cast<double>(k + 1);
+  const double theta = pi * (2.0 * j - 1.0) / (2.0 * T);
+  return 1.0 / (cfg.cheb_m + cfg.cheb_d * std::cos(theta));
+}
+
 int stepOnce(oracle_sim& s) {
   const oracle_config& cfg = s.cfg;
   const int n = s.n;
@@ -704,6 +723,7 @@ int stepOnce(oracle_sim& s) {
         for (int c = 0; c < 3; ++c) s.bBase[3 * v + c] = mh2 * s.predicted[3 * v + c];
       }
     }
+    double omega = 1.0;  // over-relaxation weight, one copy per thread (Integrator.cpp:529)
     for (int k = 0; k < cfg.max_iterations; ++k) {
       projectAndScatterInRegion(s, s.bBase.data(), s.b.data(), extra);
 #pragma omp for schedule(static, 1)
@@ -712,14 +732,24 @@ int stepOnce(oracle_sim& s) {
           if (s.pinned[v]) s.b[3 * v + c] = s.q[3 * v + c];
         solveComponent(s, c, s.b.data(), s.xSol.data(), work.data() + static_cast<size_t>(c) * n);
       }
+      const bool blend = chebBlends(cfg, k);
+      if (blend) omega = chebOmega(cfg, k, omega);
       double lDiff = 0.0, lScale = 0.0, lRes = 0.0;
       int lResV = -1;
 #pragma omp for nowait
       for (long long v = 0; v < n; ++v) {  // unpack + scan + residual (Integrator.cpp:618-663)
         const V3 xNew = ld(&s.xSol[3 * v]);
-        st(&s.x[3 * v], xNew);
-        lDiff = smax(lDiff, maxAbsComponent(sub(xNew, ld(&s.prevPos[3 * v]))));
-        st(&s.prevPos[3 * v], xNew);
+        if (blend) {  // x = x_prev + (x_solve − x_prev)·ω; the residual stays that of x_solve (:633-641)
+          const V3 xPrev = ld(&s.prevPos[3 * v]);
+          const V3 xPut = add(xPrev, mul(sub(xNew, xPrev), omega));
+          st(&s.x[3 * v], xPut);
+          lDiff = smax(lDiff, maxAbsComponent(sub(xPut, xPrev)));
+          st(&s.prevPos[3 * v], xPut);
+        } else {
+          st(&s.x[3 * v], xNew);
+          lDiff = smax(lDiff, maxAbsComponent(sub(xNew, ld(&s.prevPos[3 * v]))));
+          st(&s.prevPos[3 * v], xNew);
+        }
         lScale = smax(lScale, maxAbsComponent(sub(ld(&s.predicted[3 * v]), ld(&s.before[3 * v]))));
         if (wantResidual) {
           const double mass = s.m[v];
@@ -1219,7 +1249,8 @@ extern "C" int oracle_sim_gradient(oracle_sim* s, int substeps, const double* ta
                                    double* loss, double* dkappa, double* dv0, double* dforce) {
   ensureBuffers(*s);
   refreshFactor(*s);
-  if (!s->factorReady || substeps < 0) return -1;
+  // the over-relaxed iteration is not differentiated
+  if (!s->factorReady || substeps < 0 || s->cfg.cheb_mode != 0) return -1;
   const int n = s->n, K = s->cfg.max_iterations, ne = static_cast<int>(s->edges.size());
   const size_t dim = 3 * static_cast<size_t>(n);
   const double h = s->cfg.dt, invH2 = 1.0 / (h * h), h2 = h * h;

@@ -40,6 +40,14 @@ typedef struct oracle_config {
   double abs_tolerance;
   double residual_tolerance;
   int threads; /* 0 = all OpenMP threads */
+  /* Over-relaxation of the iterates (Integrator.cpp:476-617; the reference reads these from
+   * PD_CHEB, PD_CHEB_RHO, PD_CHEB_START, PD_CHEB_MODE, PD_CHEB_M, PD_CHEB_D):
+   * 0 off, 1 ρ recurrence after cheb_start plain iterations, 2 Chebyshev roots over [m−δ, m+δ]. */
+  int cheb_mode;
+  double cheb_rho;
+  int cheb_start;
+  double cheb_m;
+  double cheb_d;
 } oracle_config;
 
 /* Regular grid scene (restates makeGrid + makeScene, core/sim/Scene.cpp:39-177). */

@@ -2,7 +2,8 @@
 
 Sources: _verify/check.cpp:75-244 (pd_check items), tests/chain/spring_vertical.cpp,
 tests/chain/convergence_criterion.cpp, tests/primitives/test_distance_term.cpp, and the golden
-physics outputs printed in docs/perf.md:858,888,1422-1424 and docs/solver-feasibility.md:143-146.
+physics outputs printed in docs/perf.md:858,888,1422-1424, docs/solver-feasibility.md:143-146 and
+docs/chebyshev.md:280-287.
 """
 import math
 
@@ -173,6 +174,45 @@ def test_reference_bench_golden_outputs(oracle, iters, tol):
     assert st["matrix_nnz"] * 3 == 23496 and st["color_count"] == 6
     if tot is not None:
         assert sig(st["total_energy"], tot) and sig(worst, 0.0652267)
+
+
+CHEB_GOLDEN = {  # iterations -> last residual, plain PD and PD_CHEB=1 (ρ 0.98, 10 plain iterations)
+    10: (27.3033, 27.3033),
+    20: (12.3328, 9.37677),
+    40: (8.59041, 7.40925),
+    80: (6.14024, 3.51819),
+}
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("iters", list(CHEB_GOLDEN))
+def test_reference_chebyshev_golden_outputs(oracle, iters, mode):
+    """docs/chebyshev.md:280-287: pd_bench --grid 60 60 --steps 300 (κ=1e4, h=1/120, damping
+    0.02, residual gate 1e-3 never met) with and without PD_CHEB=1: the last residual."""
+    m = oracle.make_grid(oracle.GridSpec(nx=60, ny=60, spacing=0.025, stiffness=1e4))
+    s = oracle.OracleSim(m, oracle.Config(dt=1 / 120, velocity_damping=0.02, max_iterations=iters,
+                                          residual_tolerance=1e-3, cheb_mode=mode))
+    s.step(300)
+    st = s.stats()
+    assert st["early_exit_count"] == 0
+    assert sig(st["last_residual"], CHEB_GOLDEN[iters][mode])
+
+
+def test_chebyshev_weights_and_warmup(oracle):
+    """Blending starts after cheb_start plain iterations (bit-identical to plain PD before), and the
+    interval mode's roots blend from the first iteration."""
+    m = oracle.make_grid(oracle.GridSpec(nx=12, ny=12, spacing=0.025, stiffness=1e4))
+    runs = {}
+    for key, cfg in {"plain": dict(cheb_mode=0), "warm": dict(cheb_mode=1, cheb_start=12),
+                     "rho": dict(cheb_mode=1, cheb_start=3), "roots": dict(cheb_mode=2, cheb_m=0.5, cheb_d=0.45)}.items():
+        s = oracle.OracleSim(m, oracle.Config(dt=1 / 120, max_iterations=12, residual_tolerance=0.0,
+                                              rel_tolerance=0.0, abs_tolerance=0.0, **cfg))
+        s.step(20)
+        runs[key] = s.state()[0]
+    assert np.array_equal(runs["plain"], runs["warm"])  # k > cheb_start never holds with 12 iterations
+    assert not np.array_equal(runs["plain"], runs["rho"])
+    assert not np.array_equal(runs["plain"], runs["roots"])
+    assert np.all(np.isfinite(runs["roots"]))
 
 
 def test_reference_bend_golden_outputs(oracle):
