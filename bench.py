@@ -52,7 +52,7 @@ def kernel_name(info):
         return "substepDenseClusterKernel"
     if kind == 4:
         return "substepDeltaKernel"
-    return "substepCorrKernel"
+    return "substepCorrClusterKernel" if ctas > 1 else "substepCorrKernel"
 
 
 UNIT = "substeps/s"

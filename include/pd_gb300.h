@@ -79,7 +79,20 @@ typedef struct pd_scene_config {
   int32_t dense_max_vertices; /* FP32_SOLVE / MIXED with a cluster: solve with the explicit FP32
                                  inverse of Ã when every cloth has at most this many vertices
                                  (0 = PD_DENSE_DEFAULT_MAX_VERTICES, < 0 = never) */
+  /* Over-relaxed iterates, x ← x_prev + ω_k·(x_solve − x_prev), with the gate's residual taken
+   * at x_solve (core/sim/Integrator.cpp:476-645; the reference reads these from the environment
+   * variables PD_CHEB, PD_CHEB_RHO, PD_CHEB_START, PD_CHEB_MODE, PD_CHEB_M, PD_CHEB_D). */
+  int32_t cheb_mode;         /* PD_CHEB_OFF (default), PD_CHEB_RHO, PD_CHEB_INTERVAL */
+  double cheb_rho;           /* ρ of PD_CHEB_RHO (default 0.98) */
+  int32_t cheb_start;        /* plain iterations before PD_CHEB_RHO blends (default 10) */
+  double cheb_m, cheb_d;     /* PD_CHEB_INTERVAL: spectrum centre and half-width (default 1, 1) */
 } pd_scene_config;
+
+/* cheb_mode: ω_k = 2/(2−ρ²) at k = cheb_start+1, then 4/(4−ρ²·ω_{k−1}); or, from k = 0,
+ * ω_k = 1/(m + δ·cos(π(2k+1)/(2K))) with K = max_iterations. */
+#define PD_CHEB_OFF 0
+#define PD_CHEB_RHO 1
+#define PD_CHEB_INTERVAL 2
 
 #define PD_DENSE_DEFAULT_MAX_VERTICES 3072
 

@@ -27,6 +27,9 @@ PD_SOLVE_SUPERNODAL32 = 2
 PD_SOLVE_DENSE32 = 3
 PD_SOLVE_DENSE32_TEAM = 4
 PD_SOLVE_SUPERNODAL32_CORRECTION = 5
+PD_CHEB_OFF = 0                   # SceneConfig.cheb_mode: plain PD iterations
+PD_CHEB_RHO = 1                   # ω recurrence from ρ after cheb_start plain iterations (PD_CHEB=1)
+PD_CHEB_INTERVAL = 2              # Chebyshev roots over [m − δ, m + δ] (PD_CHEB_MODE=interval)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpd_gb300.so")
@@ -48,6 +51,8 @@ class _Cfg(C.Structure):
         ("bend_sampling", C.c_int32), ("bend_stride", C.c_int32), ("mass_mode", C.c_int32),
         ("total_mass", C.c_double), ("pin_mode", C.c_int32), ("precision", C.c_int32),
         ("cluster_ctas", C.c_int32), ("dense_max_vertices", C.c_int32),
+        ("cheb_mode", C.c_int32), ("cheb_rho", C.c_double), ("cheb_start", C.c_int32),
+        ("cheb_m", C.c_double), ("cheb_d", C.c_double),
     ]
 
 
@@ -219,6 +224,12 @@ class SceneConfig:
     precision: int = PD_PRECISION_FP64_EXACT
     cluster_ctas: int = 0
     dense_max_vertices: int = 0
+    # over-relaxed iterates (Integrator.cpp:476-645; the reference's PD_CHEB* variables)
+    cheb_mode: int = 0        # PD_CHEB_OFF, PD_CHEB_RHO, PD_CHEB_INTERVAL
+    cheb_rho: float = 0.98
+    cheb_start: int = 10
+    cheb_m: float = 1.0
+    cheb_d: float = 1.0
 
     def c(self) -> _Cfg:
         c = _Cfg()

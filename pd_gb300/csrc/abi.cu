@@ -89,7 +89,7 @@ struct Instance {
   std::vector<double> bendRhs;
   int factorizeCount = 0, analyzeCount = 0;
   // arena offsets
-  size_t oX, oV, oXn, oXhat, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
+  size_t oX, oV, oXn, oXhat, oXsol, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
       oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
@@ -99,6 +99,7 @@ struct Instance {
   int corrTeam = 1;     // correction kernel: CTAs (a cluster when > 1) running this instance
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
   int teamECap = 0, teamBCap = 0;
+  int teamWCap = 0;     // most window vertices of one CTA
   size_t bytes = 0;
 };
 
@@ -116,6 +117,7 @@ std::string prepare(Instance& I, bool reanalyze) {
   if (!(c.dt > 0.0)) return "dt must be positive";
   if (c.max_iterations < 0) return "max_iterations must be >= 0";
   if (!validPrecision(c.precision)) return "unsupported precision mode";
+  if (c.cheb_mode < PD_CHEB_OFF || c.cheb_mode > PD_CHEB_INTERVAL) return "cheb_mode must be 0, 1 or 2";
   std::string err = pdg::validateScene(I.scene);
   if (!err.empty()) return err;
   pdg::assembleMatrix(I.scene, c.dt, I.L);
@@ -166,14 +168,50 @@ void teamCaps(const Instance& I, int team, int* eCap, int* bCap) {
   }
 }
 
+// Team kernel: the vertex range [lo, hi) whose positions CTA r reads — its vertices, their edge
+// neighbours and bend-stencil partners — as (lo, hi) per CTA.
+std::vector<int32_t> teamWindows(const Instance& I, int team) {
+  const auto& s = I.scene;
+  std::vector<int32_t> window(2 * static_cast<size_t>(team), 0);
+  const int chunk = (s.n + team - 1) / team;
+  for (int r = 0; r < team; ++r) {
+    const int rb = std::min(s.n, r * chunk), re = std::min(s.n, rb + chunk);
+    if (rb >= re) continue;
+    int lo = rb, hi = re;
+    for (int v = rb; v < re; ++v) {
+      for (int q = I.topo.rstart[v]; q < I.topo.rstart[v + 1]; ++q) {
+        const pdg::Edge& e = s.edges[I.topo.rinc[q] >> 1];
+        lo = std::min({lo, e.a, e.b});
+        hi = std::max({hi, e.a + 1, e.b + 1});
+      }
+      for (int q = I.topo.bstart[v]; q < I.topo.bstart[v + 1]; ++q) {
+        const pdg::Bend& b = s.bends[I.topo.binc[q]];
+        lo = std::min({lo, b.a, b.b, b.c});
+        hi = std::max({hi, b.a + 1, b.b + 1, b.c + 1});
+      }
+    }
+    window[2 * r] = lo;
+    window[2 * r + 1] = hi;
+  }
+  return window;
+}
+
+int teamWindowCap(const Instance& I, int team) {
+  const std::vector<int32_t> w = teamWindows(I, team);
+  int cap = 0;
+  for (int r = 0; r < team; ++r) cap = std::max(cap, w[2 * r + 1] - w[2 * r]);
+  return cap;
+}
+
 int deltaSmem(const Instance& I, int team, int* resRows) {
   const int n = I.scene.n, ld = (n + 31) / 32 * 32, chunk = (n + team - 1) / team;
   int eCap = 0, bCap = 0;
   teamCaps(I, team, &eCap, &bCap);
+  const int wCap = teamWindowCap(I, team);
   // positions, correction, incidences, vertex constants, FP64 state, Δ, incidence offsets
   // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 24·chunk partial sums of Δ over
-  // up to two column segments)
-  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 120L * chunk + 8L * (chunk + 1);
+  // up to two column segments), and the window's previous positions (over-relaxed iterations)
+  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 120L * chunk + 8L * (chunk + 1) + 32L * wCap;
   long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (4L * ld) : 0;
   if (rows >= chunk) {
     rows = chunk;
@@ -196,7 +234,7 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
   I.oRtag = I.oXtag = I.oPtag = I.oEpoch = I.oWindow = I.oErr = I.oTEdge = I.oTBend = I.oTVtx = I.oQhl = 0;
   I.oXhl = I.oXhatHl = 0;
-  I.teamECap = I.teamBCap = 0;
+  I.teamECap = I.teamBCap = I.teamWCap = 0;
   if (denseKind == 1 || denseKind == 2) {
     I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
@@ -206,34 +244,13 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   if (denseKind == 2) {
     deltaSmem(I, teamCtas, &I.denseResRows);
     teamCaps(I, teamCtas, &I.teamECap, &I.teamBCap);
+    I.teamWCap = teamWindowCap(I, teamCtas);
     I.oRtag = A.zeros(8 * 2 * 3 * n);  // two buffers
     I.oXtag = A.zeros(8 * 6 * n);
     I.oPtag = A.zeros(8 * 3 * 16 * static_cast<size_t>(teamCtas));  // A (two buffers), B; a line each
     I.oEpoch = A.zeros(4);
     I.oErr = A.zeros(4);
-    // positions a CTA reads: its vertices, their edge neighbours and bend-stencil partners
-    std::vector<int32_t> window(2 * static_cast<size_t>(teamCtas), 0);
-    const int chunk = (s.n + teamCtas - 1) / teamCtas;
-    for (int r = 0; r < teamCtas; ++r) {
-      const int rb = std::min(s.n, r * chunk), re = std::min(s.n, rb + chunk);
-      if (rb >= re) continue;
-      int lo = rb, hi = re;
-      for (int v = rb; v < re; ++v) {
-        for (int q = I.topo.rstart[v]; q < I.topo.rstart[v + 1]; ++q) {
-          const pdg::Edge& e = s.edges[I.topo.rinc[q] >> 1];
-          lo = std::min({lo, e.a, e.b});
-          hi = std::max({hi, e.a + 1, e.b + 1});
-        }
-        for (int q = I.topo.bstart[v]; q < I.topo.bstart[v + 1]; ++q) {
-          const pdg::Bend& b = s.bends[I.topo.binc[q]];
-          lo = std::min({lo, b.a, b.b, b.c});
-          hi = std::max({hi, b.a + 1, b.b + 1, b.c + 1});
-        }
-      }
-      window[2 * r] = lo;
-      window[2 * r + 1] = hi;
-    }
-    I.oWindow = A.add(window);
+    I.oWindow = A.add(teamWindows(I, teamCtas));
   }
   if (denseKind >= 2) {
     // incidences in the kernels' FP32 form (pinned endpoints flagged in bit 31)
@@ -281,6 +298,7 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oV = A.add(s.v);
   I.oXn = A.zeros(24 * n);
   I.oXhat = A.zeros(24 * n);
+  I.oXsol = A.zeros(24 * n);
   I.oBbase = A.zeros(24 * n);
   I.oM = A.add(s.m);
   I.oPin = A.add(s.pinned);
@@ -359,7 +377,38 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.bytes = A.host.size() - before;
 }
 
-pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog) {
+// Over-relaxation weights of one substep's iterations (Integrator.cpp:529,590-617): mode ρ blends
+// from k = cheb_start + 1 with ω = 2/(2 − ρ²), then ω ← 4/(4 − ρ²·ω); the interval mode blends
+// from k = 0 with ω_k = 1/(m + δ·cos(π(2j − 1)/(2T))), j = k + 1, T = the iteration budget. The
+// weights depend on the configuration only, so they are a table computed here.
+int32_t chebFrom(const pd_scene_config& c) {
+  if (c.cheb_mode == PD_CHEB_INTERVAL) return 0;
+  if (c.cheb_mode == PD_CHEB_RHO) return c.cheb_start < 0 ? 0 : c.cheb_start + 1;
+  return INT32_MAX;
+}
+
+std::vector<double> chebWeights(const pd_scene_config& c) {
+  std::vector<double> w(std::max(0, c.max_iterations), 1.0);
+  const int from = chebFrom(c);
+  double omega = 1.0;
+  for (int k = from; k < c.max_iterations; ++k) {
+    if (c.cheb_mode == PD_CHEB_RHO) {
+      omega = (k == c.cheb_start + 1) ? 2.0 / (2.0 - c.cheb_rho * c.cheb_rho)
+                                      : 4.0 / (4.0 - c.cheb_rho * c.cheb_rho * omega);
+    } else {
+      const double pi = 3.14159265358979323846;
+      const double T = static_cast<double>(c.max_iterations);
+      const double j = static_cast<double>(k + 1);
+      const double theta = pi * (2.0 * j - 1.0) / (2.0 * T);
+      omega = 1.0 / (c.cheb_m + c.cheb_d * std::cos(theta));
+    }
+    w[k] = omega;
+  }
+  return w;
+}
+
+pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog,
+                          const double* omega) {
   auto P = [&](size_t off) { return base + off; };
   const auto& c = I.cfg;
   const auto& s = I.scene;
@@ -386,6 +435,9 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.v = reinterpret_cast<double*>(P(I.oV));
   d.xn = reinterpret_cast<double*>(P(I.oXn));
   d.xhat = reinterpret_cast<double*>(P(I.oXhat));
+  d.xsol = reinterpret_cast<double*>(P(I.oXsol));
+  d.chebFrom = chebFrom(c);
+  d.omega = omega;
   d.bbase = reinterpret_cast<double*>(P(I.oBbase));
   d.m = reinterpret_cast<const double*>(P(I.oM));
   d.pinned = reinterpret_cast<const uint8_t*>(P(I.oPin));
@@ -462,6 +514,7 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   }
   if (I.oRtag) {
     d.teamECap = I.teamECap;
+    d.teamWCap = I.teamWCap;
     d.teamBCap = I.teamBCap;
     d.rtag = reinterpret_cast<unsigned long long*>(P(I.oRtag));
     d.xtag = reinterpret_cast<unsigned long long*>(P(I.oXtag));
@@ -500,6 +553,8 @@ struct pd_sim {
   size_t arenaBytes = 0;
   pdg::InstanceDev* dDesc = nullptr;
   pdg::InstanceDev* dDescOrder = nullptr;  // batch descriptors by decreasing cost (correction kernel)
+  double* dOmega = nullptr;                // over-relaxation weights of every instance
+  size_t omegaCap = 0;
   int32_t* dIterLog = nullptr;
   uint8_t* dConvLog = nullptr;
   int logCapacity = 0;
@@ -642,11 +697,14 @@ struct pd_sim {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
     if (dDescOrder) cudaFree(dDescOrder);
+    if (dOmega) cudaFree(dOmega);
     if (dIterLog) cudaFree(dIterLog);
     if (dConvLog) cudaFree(dConvLog);
     dArena = nullptr;
     dDesc = nullptr;
     dDescOrder = nullptr;
+    dOmega = nullptr;
+    omegaCap = 0;
     dIterLog = nullptr;
     dConvLog = nullptr;
     logCapacity = 0;
@@ -681,8 +739,26 @@ struct pd_sim {
   int writeDescriptors() {
     std::vector<pdg::InstanceDev> desc;
     int smem = 0;
+    // over-relaxation weights, one table per instance
+    std::vector<double> weights;
+    std::vector<size_t> wOff(inst.size());
     for (size_t i = 0; i < inst.size(); ++i) {
-      desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity));
+      wOff[i] = weights.size();
+      const std::vector<double> w = chebWeights(inst[i].cfg);
+      weights.insert(weights.end(), w.begin(), w.end());
+    }
+    if (weights.size() > omegaCap) {
+      if (dOmega) cudaFree(dOmega);
+      dOmega = nullptr;
+      omegaCap = 0;
+      PD_CUDA(cudaMalloc(&dOmega, sizeof(double) * weights.size()));
+      omegaCap = weights.size();
+    }
+    if (!weights.empty())
+      PD_CUDA(cudaMemcpy(dOmega, weights.data(), sizeof(double) * weights.size(), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < inst.size(); ++i) {
+      desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity,
+                              dOmega ? dOmega + wOff[i] : nullptr));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
       int rows = 0;
       const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
@@ -891,6 +967,11 @@ void pd_scene_config_default(pd_scene_config* c) {
   c->bend_stride = 1;
   c->total_mass = 1.0;
   c->precision = PD_PRECISION_FP64_EXACT;
+  c->cheb_mode = PD_CHEB_OFF;
+  c->cheb_rho = 0.98;
+  c->cheb_start = 10;
+  c->cheb_m = 1.0;
+  c->cheb_d = 1.0;
 }
 
 int pd_grid_counts(const pd_scene_config* cfg, int32_t* nv, int32_t* ne, int32_t* nb) {
@@ -1160,6 +1241,8 @@ int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
   if (!(cfg->dt > 0.0) || cfg->max_iterations < 0) return fail(PD_ERR_INVALID_ARGUMENT, "invalid dt or iteration count");
   if (!validPrecision(cfg->precision))
     return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
+  if (cfg->cheb_mode < PD_CHEB_OFF || cfg->cheb_mode > PD_CHEB_INTERVAL)
+    return fail(PD_ERR_INVALID_ARGUMENT, "cheb_mode must be 0, 1 or 2");
   bool refactor = false;
   for (auto& I : s->inst) {
     refactor = refactor || (std::memcmp(&I.cfg.dt, &cfg->dt, sizeof(double)) != 0);
@@ -1194,7 +1277,7 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   out->factorize_count = I.factorizeCount;
   out->analyze_count = I.analyzeCount;
   out->device_bytes = static_cast<int64_t>(I.bytes);
-  out->cluster_ctas = s->teamCtas;
+  out->cluster_ctas = (s->corr && I.corrTeam > 1) ? I.corrTeam : s->teamCtas;
   const int p = s->precision();
   out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                     : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
@@ -1279,6 +1362,9 @@ int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, c
   const int count = static_cast<int>(s->inst.size());
   for (int i = 0; i < count; ++i)
     if (!targets[i]) return fail(PD_ERR_INVALID_ARGUMENT, "null target of instance " + std::to_string(i));
+  for (const auto& I : s->inst)
+    if (I.cfg.cheb_mode != PD_CHEB_OFF)
+      return fail(PD_ERR_UNSUPPORTED, "gradients of over-relaxed iterations (cheb_mode) are not provided");
   if (const int rc_ = s->sync()) return rc_;
   // device work arrays: per instance [target, force?, checkpoints, iterates, state and adjoints,
   // per-edge terms, loss]

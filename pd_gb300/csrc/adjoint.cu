@@ -53,7 +53,7 @@ __device__ void forwardSubstep(const InstanceDev& J, const GradDev& G, const Tea
       if (it) it[3 * v + c] = p;
     }
   }
-  for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, e, false);
+  for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, J.x, e, false);
   __syncthreads();
   for (int k = 0; k < J.maxIter; ++k) {
     for (int v = threadIdx.x; v < n; v += blockDim.x) gatherRow(J, tm, v, w);
@@ -67,7 +67,7 @@ __device__ void forwardSubstep(const InstanceDev& J, const GradDev& G, const Tea
       }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, e, false);
+    for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, J.x, e, false);
     __syncthreads();
   }
   for (int v = threadIdx.x; v < n; v += blockDim.x) {  // velocity, damping, pin resnap

@@ -23,11 +23,16 @@ struct InstanceDev {
   double gScaleHH;       // |g|·h·h
   double resThreshold;   // residual_tolerance · max(|g|, 1e−12)
   double relTol, absTol;
+  // over-relaxed iterates (Integrator.cpp:476-645): iteration k ≥ chebFrom puts
+  // x_prev + ω_k·(x_solve − x_prev) and gates on the residual of x_solve
+  int32_t chebFrom;      // INT32_MAX: plain PD
+  const double* omega;   // maxIter weights ω_k
   // vertex state (3n interleaved unless noted)
   double* x;
   double* v;
   double* xn;            // positions at the start of the substep
   double* xhat;          // predicted positions
+  double* xsol;          // the solve's result before over-relaxation (residual point)
   double* bbase;         // (M/h²)·x̂
   const double* m;       // n
   const uint8_t* pinned; // n
@@ -99,6 +104,7 @@ struct InstanceDev {
   // (epoch << 32 | FP32 bits): a reader knows a word is current from its epoch alone.
   int32_t denseResRows;        // rows of Ã⁻¹ a CTA keeps in shared memory (multiple of 4 unless all)
   int32_t teamECap, teamBCap;  // most edge / bend incidences of one CTA's vertices
+  int32_t teamWCap;            // most window vertices of one CTA
   const int4* tEdge;           // per edge incidence (rstart order): other | pinned << 31, rest, κ (FP32 bits), 0
   const int4* tBend;           // per bend incidence (bstart order): a, b, c (| pinned << 31), (−k)·w_v bits
   const float4* tVtx;          // per vertex: m/h², 1/m (0 when m ≤ 0), pinned, 0

@@ -59,13 +59,14 @@ __device__ __forceinline__ double maxAbs3(double a, double b, double c) {
 
 // d_e = ℓ·(x_a − x_b)/‖x_a − x_b‖ (0 when degenerate), DistanceTerm.cpp:94-102;
 // kd = κ·d (scatter term, DistanceTerm.cpp:121-152); rc = κ·rel − κ·d (Integrator.cpp:246-248).
+// X: the positions (I.x, or I.xsol for the residual of an over-relaxed iteration).
 template <class A>
-__device__ void edgePass(const InstanceDev& I, bool wantRc) {
+__device__ void edgePass(const InstanceDev& I, const double* X, bool wantRc) {
   for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
     const int a = I.eab[2 * e], b = I.eab[2 * e + 1];
-    const double rx = A::sub(I.x[3 * a], I.x[3 * b]);
-    const double ry = A::sub(I.x[3 * a + 1], I.x[3 * b + 1]);
-    const double rz = A::sub(I.x[3 * a + 2], I.x[3 * b + 2]);
+    const double rx = A::sub(X[3 * a], X[3 * b]);
+    const double ry = A::sub(X[3 * a + 1], X[3 * b + 1]);
+    const double rz = A::sub(X[3 * a + 2], X[3 * b + 2]);
     const double len = A::sqrt(A::add(A::add(A::mul(rx, rx), A::mul(ry, ry)), A::mul(rz, rz)));
     double dx = 0.0, dy = 0.0, dz = 0.0;
     if (!(len <= 1e-12)) {
@@ -139,9 +140,9 @@ __device__ void gatherRhs(const InstanceDev& I, double* w) {
   }
 }
 
-// Nonlinear residual of vertex v at the current positions (Integrator.cpp:230-263).
+// Nonlinear residual of vertex v at positions X (Integrator.cpp:230-263).
 template <class A>
-__device__ double vertexResidual(const InstanceDev& I, int v) {
+__device__ double vertexResidual(const InstanceDev& I, const double* X, int v) {
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
   for (int k = I.rstart[v]; k < I.rstart[v + 1]; ++k) {
     const int p = I.rinc[k];
@@ -161,9 +162,9 @@ __device__ double vertexResidual(const InstanceDev& I, int v) {
     const int s = I.binc[k];
     const int a = I.babc[3 * s], b = I.babc[3 * s + 1], c = I.babc[3 * s + 2];
     const double fac = I.bfac[k];
-    const double s0 = A::add(A::sub(I.x[3 * a], A::mul(2.0, I.x[3 * b])), I.x[3 * c]);
-    const double s1 = A::add(A::sub(I.x[3 * a + 1], A::mul(2.0, I.x[3 * b + 1])), I.x[3 * c + 1]);
-    const double s2 = A::add(A::sub(I.x[3 * a + 2], A::mul(2.0, I.x[3 * b + 2])), I.x[3 * c + 2]);
+    const double s0 = A::add(A::sub(X[3 * a], A::mul(2.0, X[3 * b])), X[3 * c]);
+    const double s1 = A::add(A::sub(X[3 * a + 1], A::mul(2.0, X[3 * b + 1])), X[3 * c + 1]);
+    const double s2 = A::add(A::sub(X[3 * a + 2], A::mul(2.0, X[3 * b + 2])), X[3 * c + 2]);
     g0 = A::add(g0, A::mul(s0, fac));
     g1 = A::add(g1, A::mul(s1, fac));
     g2 = A::add(g2, A::mul(s2, fac));
@@ -173,9 +174,9 @@ __device__ double vertexResidual(const InstanceDev& I, int v) {
   f2 = A::add(f2, g2);
   const double mass = I.m[v];
   const double mh2 = A::mul(mass, I.invH2);
-  const double t0 = A::add(A::mul(A::sub(I.x[3 * v], I.xhat[3 * v]), mh2), f0);
-  const double t1 = A::add(A::mul(A::sub(I.x[3 * v + 1], I.xhat[3 * v + 1]), mh2), f1);
-  const double t2 = A::add(A::mul(A::sub(I.x[3 * v + 2], I.xhat[3 * v + 2]), mh2), f2);
+  const double t0 = A::add(A::mul(A::sub(X[3 * v], I.xhat[3 * v]), mh2), f0);
+  const double t1 = A::add(A::mul(A::sub(X[3 * v + 1], I.xhat[3 * v + 1]), mh2), f1);
+  const double t2 = A::add(A::mul(A::sub(X[3 * v + 2], I.xhat[3 * v + 2]), mh2), f2);
   const double len = A::sqrt(A::add(A::add(A::mul(t0, t0), A::mul(t1, t1)), A::mul(t2, t2)));
   return A::div(len, mass);
 }
@@ -204,7 +205,7 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
     scale = blockMax(scale, red);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
 
-    edgePass<A>(I, false);  // projection of x_n for the first scatter
+    edgePass<A>(I, I.x, false);  // projection of x_n for the first scatter
     __syncthreads();
     int used = 0;
     bool conv = false;
@@ -213,27 +214,49 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
       gatherRhs<A>(I, w);
       __syncthreads();
       Solve::run(I, w, t);
-      // unpack + displacement scan (Integrator.cpp:618-663)
+      // unpack + displacement scan (Integrator.cpp:618-663); an over-relaxed iteration puts
+      // x_prev + (x_solve − x_prev)·ω and keeps x_solve for the residual (:631-641)
+      const bool blend = k >= I.chebFrom;
+      const bool split = blend && I.useResidual;
+      const double om = blend ? I.omega[k] : 1.0;
       double diff = 0.0;
       for (int v = threadIdx.x; v < I.n; v += blockDim.x) {
         const int r = I.iperm[v];
-        const double x0 = w[3 * r], x1 = w[3 * r + 1], x2 = w[3 * r + 2];
-        diff = fmax(diff, maxAbs3(A::sub(x0, I.x[3 * v]), A::sub(x1, I.x[3 * v + 1]), A::sub(x2, I.x[3 * v + 2])));
-        I.x[3 * v] = x0;
-        I.x[3 * v + 1] = x1;
-        I.x[3 * v + 2] = x2;
+        double xs[3] = {w[3 * r], w[3 * r + 1], w[3 * r + 2]};
+        if (blend) {
+          double d[3];
+          for (int c = 0; c < 3; ++c) {
+            const double p = I.x[3 * v + c];
+            const double put = A::add(p, A::mul(A::sub(xs[c], p), om));
+            d[c] = A::sub(put, p);
+            if (split) I.xsol[3 * v + c] = xs[c];
+            I.x[3 * v + c] = put;
+          }
+          diff = fmax(diff, maxAbs3(d[0], d[1], d[2]));
+        } else {
+          diff = fmax(diff, maxAbs3(A::sub(xs[0], I.x[3 * v]), A::sub(xs[1], I.x[3 * v + 1]),
+                                    A::sub(xs[2], I.x[3 * v + 2])));
+          I.x[3 * v] = xs[0];
+          I.x[3 * v + 1] = xs[1];
+          I.x[3 * v + 2] = xs[2];
+        }
       }
       __syncthreads();
-      edgePass<A>(I, I.useResidual != 0);
+      const double* X = split ? I.xsol : I.x;
+      edgePass<A>(I, X, I.useResidual != 0);
       __syncthreads();
       double res = 0.0;
       if (I.useResidual) {
         for (int v = threadIdx.x; v < I.n; v += blockDim.x) {
           if (I.pinned[v] || !(I.m[v] > 0.0)) continue;
-          const double r = vertexResidual<A>(I, v);
+          const double r = vertexResidual<A>(I, X, v);
           if (r > res) res = r;
         }
-        res = blockMax(res, red);
+        res = blockMax(res, red);  // ends with a barrier: rc is no longer read below
+      }
+      if (split) {  // the next scatter projects the over-relaxed positions
+        edgePass<A>(I, I.x, false);
+        __syncthreads();
       }
       diff = blockMax(diff, red);
       // gate (Integrator.cpp:676-747)

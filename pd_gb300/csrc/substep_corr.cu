@@ -215,8 +215,9 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
     int used = 0;
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
-    for (int k = 0;; ++k) {
-      // correction (elimination order, into Y) and residual of x^k
+    // correction b − Ã·x (elimination order, into Y when wanted) and the largest residual of the
+    // current positions, 8 lanes per vertex
+    auto correctionPass = [&](bool wantY) {
       float res = 0.f;
       for (int base = 0; base < n; base += ngroups) {
         const int v = base + group;
@@ -236,15 +237,22 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
             if (vc.y > 0.f) res = fmaxf(res, cs.residual(vc.y));
             r = cs.correction();
           }
-          const int e = I.iperm[v];
-          Y[3 * e] = r.x;
-          Y[3 * e + 1] = r.y;
-          Y[3 * e + 2] = r.z;
+          if (wantY) {
+            const int e = I.iperm[v];
+            Y[3 * e] = r.x;
+            Y[3 * e + 1] = r.y;
+            Y[3 * e + 2] = r.z;
+          }
         }
       }
-      const double resMax = teamMax(tm, static_cast<double>(res), red, slots, parity);
+      return teamMax(tm, static_cast<double>(res), red, slots, parity);
+    };
+    for (int k = 0;; ++k) {
+      // correction and residual of x^k; the residual gates iteration k − 1 unless that iteration
+      // was over-relaxed and gated on its own solve's residual below
+      const double resMax = correctionPass(true);
       bool stop = k == I.maxIter;
-      if (I.useResidual && k >= 1) {
+      if (I.useResidual && k >= 1 && k - 1 < I.chebFrom) {
         lastRes = resMax;
         used = k;
         conv = resMax <= I.resThreshold;
@@ -252,24 +260,50 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       }
       if (stop) break;
       TeamSolve32<CLUSTER>::run(I, tm, Y, T);  // Y ← Δ
-      // x^{k+1} = x^k + Δ as pairs; pinned rows take q
+      // x^{k+1} = x^k + Δ as pairs; pinned rows take q. An over-relaxed iteration
+      // (Integrator.cpp:631-641) puts x^k + ω·Δ; with the residual gate it first puts x^k + Δ,
+      // takes that point's residual, then adds (ω − 1)·Δ.
+      const bool blend = k >= I.chebFrom;
+      const bool split = blend && I.useResidual;
+      const float om = blend ? static_cast<float>(I.omega[k]) : 1.f;
       double dmax = 0.0;
       for (int t = TID; t < n3; t += NT) {
         const int v = t / 3, c = t - 3 * v;
         float hi = tm.ld(xf + 8 * v + c), lo = tm.ld(xf + 8 * v + 4 + c);
+        float* y = Y + 3 * I.iperm[v] + c;
+        float d;
         if (I.pinned[v]) {
           const float* qf = reinterpret_cast<const float*>(I.qhl);
           const float qh = __ldg(qf + 8 * v + c), ql = __ldg(qf + 8 * v + 4 + c);
-          dmax = fmax(dmax, static_cast<double>(fabsf((qh - hi) + (ql - lo))));
+          d = (qh - hi) + (ql - lo);
           hi = qh;
           lo = ql;
+          if (blend && !split) addHL(hi, lo, (om - 1.f) * d);
+          if (split) *y = d;
         } else {
-          const float d = tm.ld(Y + 3 * I.iperm[v] + c);
-          dmax = fmax(dmax, static_cast<double>(fabsf(d)));
-          addHL(hi, lo, d);
+          d = tm.ld(y);
+          addHL(hi, lo, split ? d : om * d);
         }
+        dmax = fmax(dmax, static_cast<double>(fabsf(blend ? om * d : d)));
         xf[8 * v + c] = hi;
         xf[8 * v + 4 + c] = lo;
+      }
+      if (split) {
+        tm.sync();
+        const double resSolve = correctionPass(false);  // residual of x^k + Δ; ends with a team barrier
+        for (int t = TID; t < n3; t += NT) {
+          const int v = t / 3, c = t - 3 * v;
+          float hi = tm.ld(xf + 8 * v + c), lo = tm.ld(xf + 8 * v + 4 + c);
+          addHL(hi, lo, (om - 1.f) * tm.ld(Y + 3 * I.iperm[v] + c));
+          xf[8 * v + c] = hi;
+          xf[8 * v + 4 + c] = lo;
+        }
+        tm.sync();
+        lastRes = resSolve;
+        used = k + 1;
+        conv = resSolve <= I.resThreshold;
+        if (conv || k + 1 == I.maxIter) break;
+        continue;
       }
       const double diff = teamMax(tm, dmax, red, slots, parity);
       if (!I.useResidual) {

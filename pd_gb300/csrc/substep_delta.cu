@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   int4* sB = sE + I.teamECap;
   float4* sV = reinterpret_cast<float4*>(sB + I.teamBCap);
   float4* sXh = sV + chunk;
-  double* xn64 = reinterpret_cast<double*>(sXh + 2 * chunk);
+  float4* sXp = sXh + 2 * chunk;  // window positions before an over-relaxed update (teamWCap pairs)
+  double* xn64 = reinterpret_cast<double*>(sXp + 2 * I.teamWCap);
   double* v64 = xn64 + 3 * chunk;
   float* dl = reinterpret_cast<float*>(v64 + 3 * chunk);  // kSegments × 3·chunk
   int* sEb = reinterpret_cast<int*>(dl + kSegments * 3 * chunk);
@@ -285,7 +286,16 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     int used = 0;
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
+    float resSplit = 0.f;  // residual of the last over-relaxed iteration's solve (per thread)
     for (int k = 0;; ++k) {
+      // an over-relaxed iteration with the residual gate (Integrator.cpp:631-663) puts x^k + Δ,
+      // takes that point's residual, then adds (ω − 1)·Δ to every window vertex
+      const bool blend = k >= I.chebFrom && k < I.maxIter;
+      const bool split = blend && I.useResidual;
+      const bool splitBefore = I.useResidual && k >= 1 && k - 1 >= I.chebFrom;
+      const float om = blend ? static_cast<float>(I.omega[k]) : 1.f;
+      if (split)
+        for (int t = threadIdx.x; t < 2 * (whi - wlo); t += blockDim.x) sXp[t] = Xs[2 * wlo + t];
       const unsigned tagA = ++epoch;  // odd: epochs are consumed in (A, B) pairs
       const unsigned buf = (tagA >> 1) & 1u;
       unsigned long long* rtag = I.rtag + buf * 3 * n;
@@ -318,6 +328,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       }
       // exchange A, a full barrier of the team: the whole correction (warps 1..) and the maximum
       // of the residuals — at k = 0 of the scale — (warp 0)
+      if (splitBefore) resLocal = resSplit;  // iteration k − 1 is gated on its solve's residual
       resLocal = warpMaxF(resLocal);
       if (lane == 0) red[warp] = (k == 0) ? scW : resLocal;
       __syncthreads();
@@ -375,14 +386,16 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         if (sV[li].z != 0.f) {
           const float* qf = reinterpret_cast<const float*>(I.qhl);
           const float qh = __ldg(qf + 8 * v + c), ql = __ldg(qf + 8 * v + 4 + c);
-          dmax = fmaxf(dmax, fabsf((qh - hi) + (ql - lo)));
+          const float d = (qh - hi) + (ql - lo);
+          dmax = fmaxf(dmax, fabsf(om * d));
           hi = qh;
           lo = ql;
+          if (blend && !split) addHL(hi, lo, (om - 1.f) * d);
         } else {
           float d = dl[t];
           for (int sgi = 1; sgi < segs; ++sgi) d += dl[sgi * 3 * chunk + t];
-          dmax = fmaxf(dmax, fabsf(d));
-          addHL(hi, lo, d);
+          dmax = fmaxf(dmax, fabsf(om * d));
+          addHL(hi, lo, (blend && !split) ? om * d : d);
         }
         storeRelaxed(I.xtag + 6 * v + c, tagged(tagB, hi));
         storeRelaxed(I.xtag + 6 * v + 3 + c, tagged(tagB, lo));
@@ -418,6 +431,38 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
+      if (split) {
+        // residual of x^k + Δ for own vertices, sent with the next exchange A
+        resSplit = 0.f;
+        for (int base = 0; base < m; base += ngroups) {
+          const int li = base + group;
+          const bool active = li < m;
+          const float4 vc = active ? sV[li] : make_float4(0.f, 0.f, 1.f, 0.f);
+          const int v = rb + li;
+          CorrectionSums cs;
+          if (vc.z == 0.f) {
+            const float4 vh = Xs[2 * v], vl = Xs[2 * v + 1];
+            cs.accumulate(I, sE, sEb[li], sEb[li + 1], sB, sBb[li], sBb[li + 1], Xs, vh, vl, gl, kGroup);
+            if (gl == 0) cs.addMass(vh, vl, sXh[2 * li], sXh[2 * li + 1], vc.x);
+          }
+          cs.reduce<kGroup>();
+          if (active && gl == 0 && vc.z == 0.f && vc.y > 0.f) resSplit = fmaxf(resSplit, cs.residual(vc.y));
+        }
+        __syncthreads();
+        // x^{k+1} = (x^k + Δ) + (ω − 1)·Δ over the whole window, Δ recovered from the pairs, so
+        // that every CTA reading a vertex computes the same bits as its owner
+        for (int j = threadIdx.x; j < whi - wlo; j += blockDim.x) {
+          const int v = wlo + j;
+          float4 h = Xs[2 * v], l = Xs[2 * v + 1];
+          const float3 d = diffHL(h, l, sXp[2 * j], sXp[2 * j + 1]);
+          addHL(h.x, l.x, (om - 1.f) * d.x);
+          addHL(h.y, l.y, (om - 1.f) * d.y);
+          addHL(h.z, l.z, (om - 1.f) * d.z);
+          Xs[2 * v] = h;
+          Xs[2 * v + 1] = l;
+        }
+        __syncthreads();
+      }
       if (!I.useResidual) {
         const double diff = gate;
         const double rel = (scale > 0.0) ? diff / scale : diff;

@@ -63,7 +63,7 @@ __device__ void runSubstepsMixed(const InstanceDev& I, const Team<CLUSTER>& tm, 
     }
     scale = teamMax(tm, scale, red, slots, parity);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
-    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, e, false);  // projection of x_n
+    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);  // projection of x_n
     tm.sync();
     int used = 0;
     bool conv = false;
@@ -137,20 +137,28 @@ __device__ void runSubstepsMixed(const InstanceDev& I, const Team<CLUSTER>& tm, 
       LocalSolve32::run(I, Y, Tt);
       for (int i = threadIdx.x; i < n3; i += blockDim.x) X0[i] += static_cast<double>(Y[i]);
       __syncthreads();
-      // unpack this CTA's vertices + displacement scan (Integrator.cpp:618-663)
+      // unpack this CTA's vertices + displacement scan (Integrator.cpp:618-663); an over-relaxed
+      // iteration puts x_prev + (x_solve − x_prev)·ω, the residual below stays that of x_solve (X0)
+      const bool blend = k >= I.chebFrom;
+      const double om = blend ? I.omega[k] : 1.0;
       double diff = 0.0;
       for (int v = T; v < I.n; v += NT) {
         const int r = I.iperm[v];
         double dm = 0.0;
         for (int c = 0; c < 3; ++c) {
-          const double xn = X0[3 * r + c];
-          dm = fmax(dm, fabs(xn - tm.ld(I.x + 3 * v + c)));
-          I.x[3 * v + c] = xn;
+          const double xs = X0[3 * r + c], p = tm.ld(I.x + 3 * v + c);
+          const double put = blend ? p + (xs - p) * om : xs;
+          dm = fmax(dm, fabs(put - p));
+          I.x[3 * v + c] = put;
         }
         diff = fmax(diff, dm);
       }
       for (int e = T; e < I.ne; e += NT) edgeTermsElim(I, X0, e, I.useResidual != 0);
       tm.sync();
+      if (blend) {  // the next right-hand side projects the over-relaxed positions (rc is kept)
+        for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);
+        tm.sync();
+      }
       double res = 0.0;
       if (I.useResidual) {
         for (int v = T; v < I.n; v += NT) {
@@ -272,7 +280,7 @@ __device__ void runSubstepsDense(const InstanceDev& I, const Team<true>& tm, int
     }
     scale = teamMax(tm, scale, red, slots, parity);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
-    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, e, false);  // projection of x_n
+    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);  // projection of x_n
     tm.sync();
     int used = 0;
     bool conv = false;
@@ -335,25 +343,41 @@ __device__ void runSubstepsDense(const InstanceDev& I, const Team<true>& tm, int
         Sz[v] = static_cast<float>(__ldcg(I.x0 + 3 * v + 2));
       }
       __syncthreads();
+      // x_solve = x₀ + Ã⁻¹·r; an over-relaxed iteration puts x_prev + (x_solve − x_prev)·ω and
+      // keeps x_solve for the residual (Integrator.cpp:631-641)
+      const bool blend = k >= I.chebFrom;
+      const bool split = blend && I.useResidual;
+      const double om = blend ? I.omega[k] : 1.0;
       double diff = 0.0;
-      denseRows(I, rb, re, Sx, Sy, Sz, [&](int i, float a0, float a1, float a2) {  // x = x₀ + Ã⁻¹·r
-        const double x0 = X0[3 * i] + a0, x1 = X0[3 * i + 1] + a1, x2 = X0[3 * i + 2] + a2;
-        diff = fmax(diff, maxAbs3(x0 - __ldcg(I.x + 3 * i), x1 - __ldcg(I.x + 3 * i + 1), x2 - __ldcg(I.x + 3 * i + 2)));
-        __stcg(I.x + 3 * i, x0);
-        __stcg(I.x + 3 * i + 1, x1);
-        __stcg(I.x + 3 * i + 2, x2);
+      denseRows(I, rb, re, Sx, Sy, Sz, [&](int i, float a0, float a1, float a2) {
+        const float a[3] = {a0, a1, a2};
+        for (int c = 0; c < 3; ++c) {
+          const double xs = X0[3 * i + c] + a[c], p = __ldcg(I.x + 3 * i + c);
+          double put = xs;
+          if (blend) {
+            put = p + (xs - p) * om;
+            if (split) __stcg(I.xsol + 3 * i + c, xs);
+          }
+          diff = fmax(diff, fabs(put - p));
+          __stcg(I.x + 3 * i + c, put);
+        }
       });
       tm.sync();
-      for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, e, I.useResidual != 0);
+      const double* X = split ? I.xsol : I.x;
+      for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, X, e, I.useResidual != 0);
       tm.sync();
       double res = 0.0;
       if (I.useResidual) {
         for (int v = T; v < n; v += NT) {
           if (I.pinned[v] || !(I.m[v] > 0.0)) continue;
-          const double r = residualAt(I, tm, v);
+          const double r = residualAt(I, tm, X, v);
           if (r > res) res = r;
         }
         res = teamMax(tm, res, red, slots, parity);
+      }
+      if (split) {  // the next right-hand side projects the over-relaxed positions
+        for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);
+        tm.sync();
       }
       diff = teamMax(tm, diff, red, slots, parity);
       const double rel = (scale > 0.0) ? diff / scale : diff;

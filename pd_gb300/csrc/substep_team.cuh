@@ -73,14 +73,15 @@ __device__ __forceinline__ void projectEdge(const InstanceDev& I, int e, double 
   }
 }
 
-// Edge e at the current positions: κ·d_e and κ·rel − κ·d_e (DistanceTerm.cpp:94-152,
-// Integrator.cpp:246-248).
+// Edge e at positions X (I.x, or I.xsol for the residual of an over-relaxed iteration): κ·d_e and
+// κ·rel − κ·d_e (DistanceTerm.cpp:94-152, Integrator.cpp:246-248).
 template <bool CLUSTER>
-__device__ __forceinline__ void edgeTerms(const InstanceDev& I, const Team<CLUSTER>& tm, int e, bool wantRc) {
+__device__ __forceinline__ void edgeTerms(const InstanceDev& I, const Team<CLUSTER>& tm, const double* X, int e,
+                                          bool wantRc) {
   const int a = I.eab[2 * e], b = I.eab[2 * e + 1];
-  const double rx = tm.ld(I.x + 3 * a) - tm.ld(I.x + 3 * b);
-  const double ry = tm.ld(I.x + 3 * a + 1) - tm.ld(I.x + 3 * b + 1);
-  const double rz = tm.ld(I.x + 3 * a + 2) - tm.ld(I.x + 3 * b + 2);
+  const double rx = tm.ld(X + 3 * a) - tm.ld(X + 3 * b);
+  const double ry = tm.ld(X + 3 * a + 1) - tm.ld(X + 3 * b + 1);
+  const double rz = tm.ld(X + 3 * a + 2) - tm.ld(X + 3 * b + 2);
   double dx = 0.0, dy = 0.0, dz = 0.0;
   projectEdge(I, e, rx, ry, rz, dx, dy, dz);
   const double k = I.ek[e];
@@ -134,9 +135,9 @@ __device__ __forceinline__ void gatherRow(const InstanceDev& I, const Team<CLUST
   w[3 * r + 2] = b2;
 }
 
-// Nonlinear residual of vertex v (Integrator.cpp:230-263).
+// Nonlinear residual of vertex v at positions X (Integrator.cpp:230-263).
 template <bool CLUSTER>
-__device__ __forceinline__ double residualAt(const InstanceDev& I, const Team<CLUSTER>& tm, int v) {
+__device__ __forceinline__ double residualAt(const InstanceDev& I, const Team<CLUSTER>& tm, const double* X, int v) {
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
   for (int k = I.rstart[v]; k < I.rstart[v + 1]; ++k) {
     const int p = I.rinc[k];
@@ -150,15 +151,15 @@ __device__ __forceinline__ double residualAt(const InstanceDev& I, const Team<CL
     const int s = I.binc[k];
     const int a = I.babc[3 * s], b = I.babc[3 * s + 1], c = I.babc[3 * s + 2];
     const double fac = I.bfac[k];
-    f0 = fma(tm.ld(I.x + 3 * a) - 2.0 * tm.ld(I.x + 3 * b) + tm.ld(I.x + 3 * c), fac, f0);
-    f1 = fma(tm.ld(I.x + 3 * a + 1) - 2.0 * tm.ld(I.x + 3 * b + 1) + tm.ld(I.x + 3 * c + 1), fac, f1);
-    f2 = fma(tm.ld(I.x + 3 * a + 2) - 2.0 * tm.ld(I.x + 3 * b + 2) + tm.ld(I.x + 3 * c + 2), fac, f2);
+    f0 = fma(tm.ld(X + 3 * a) - 2.0 * tm.ld(X + 3 * b) + tm.ld(X + 3 * c), fac, f0);
+    f1 = fma(tm.ld(X + 3 * a + 1) - 2.0 * tm.ld(X + 3 * b + 1) + tm.ld(X + 3 * c + 1), fac, f1);
+    f2 = fma(tm.ld(X + 3 * a + 2) - 2.0 * tm.ld(X + 3 * b + 2) + tm.ld(X + 3 * c + 2), fac, f2);
   }
   const double mass = I.m[v];
   const double mh2 = mass * I.invH2;
-  const double t0 = fma(tm.ld(I.x + 3 * v) - tm.ld(I.xhat + 3 * v), mh2, f0);
-  const double t1 = fma(tm.ld(I.x + 3 * v + 1) - tm.ld(I.xhat + 3 * v + 1), mh2, f1);
-  const double t2 = fma(tm.ld(I.x + 3 * v + 2) - tm.ld(I.xhat + 3 * v + 2), mh2, f2);
+  const double t0 = fma(tm.ld(X + 3 * v) - tm.ld(I.xhat + 3 * v), mh2, f0);
+  const double t1 = fma(tm.ld(X + 3 * v + 1) - tm.ld(I.xhat + 3 * v + 1), mh2, f1);
+  const double t2 = fma(tm.ld(X + 3 * v + 2) - tm.ld(I.xhat + 3 * v + 2), mh2, f2);
   return sqrt(t0 * t0 + t1 * t1 + t2 * t2) / mass;
 }
 
@@ -345,7 +346,7 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
     }
     scale = teamMax(tm, scale, red, slots, parity);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
-    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, e, false);  // projection of x_n
+    for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);  // projection of x_n
     tm.sync();
     int used = 0;
     bool conv = false;
@@ -354,26 +355,41 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
       for (int v = T; v < I.n; v += NT) gatherRow(I, tm, v, w);
       tm.sync();
       TeamSolve<CLUSTER>::run(I, tm, w, t);
+      // unpack + displacement scan; an over-relaxed iteration puts x_prev + (x_solve − x_prev)·ω
+      // and keeps x_solve for the residual (Integrator.cpp:631-641)
+      const bool blend = k >= I.chebFrom;
+      const bool split = blend && I.useResidual;
+      const double om = blend ? I.omega[k] : 1.0;
       double diff = 0.0;
-      for (int v = T; v < I.n; v += NT) {  // unpack + displacement scan
+      for (int v = T; v < I.n; v += NT) {
         const int r = I.iperm[v];
-        const double x0 = tm.ld(w + 3 * r), x1 = tm.ld(w + 3 * r + 1), x2 = tm.ld(w + 3 * r + 2);
-        diff = fmax(diff, maxAbs3(x0 - tm.ld(I.x + 3 * v), x1 - tm.ld(I.x + 3 * v + 1), x2 - tm.ld(I.x + 3 * v + 2)));
-        I.x[3 * v] = x0;
-        I.x[3 * v + 1] = x1;
-        I.x[3 * v + 2] = x2;
+        for (int c = 0; c < 3; ++c) {
+          const double xs = tm.ld(w + 3 * r + c), p = tm.ld(I.x + 3 * v + c);
+          double put = xs;
+          if (blend) {
+            put = p + (xs - p) * om;
+            if (split) I.xsol[3 * v + c] = xs;
+          }
+          diff = fmax(diff, fabs(put - p));
+          I.x[3 * v + c] = put;
+        }
       }
       tm.sync();
-      for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, e, I.useResidual != 0);
+      const double* X = split ? I.xsol : I.x;
+      for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, X, e, I.useResidual != 0);
       tm.sync();
       double res = 0.0;
       if (I.useResidual) {
         for (int v = T; v < I.n; v += NT) {
           if (I.pinned[v] || !(I.m[v] > 0.0)) continue;
-          const double r = residualAt(I, tm, v);
+          const double r = residualAt(I, tm, X, v);
           if (r > res) res = r;
         }
         res = teamMax(tm, res, red, slots, parity);
+      }
+      if (split) {  // the next scatter projects the over-relaxed positions
+        for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);
+        tm.sync();
       }
       diff = teamMax(tm, diff, red, slots, parity);
       // gate (Integrator.cpp:676-747): every thread holds the reduced values and decides alike

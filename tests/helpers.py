@@ -8,7 +8,8 @@ def oracle_config(cfg, threads=0):
     return O.Config(dt=cfg.dt, gravity=tuple(cfg.gravity), velocity_damping=cfg.velocity_damping,
                     max_iterations=cfg.max_iterations, rel_tolerance=cfg.rel_tolerance,
                     abs_tolerance=cfg.abs_tolerance, residual_tolerance=cfg.residual_tolerance,
-                    threads=threads)
+                    threads=threads, cheb_mode=cfg.cheb_mode, cheb_rho=cfg.cheb_rho,
+                    cheb_start=cfg.cheb_start, cheb_m=cfg.cheb_m, cheb_d=cfg.cheb_d)
 
 
 def oracle_twin(scene, cfg, perm=None, threads=0):

@@ -109,3 +109,19 @@ def test_workloads_are_deterministic(pdg):
     s, cfg, sub = W.cloth40_full()
     assert s[0].edges.shape[0] == 4641 and s[0].bends.shape[0] == 3040 and sub == 600
     assert abs(s[0].masses.sum() - 1.0) < 1e-12
+
+
+def test_config_defaults_match_the_c_abi(pdg):
+    """pd_scene_config_default and the Python SceneConfig agree field by field (incl. the
+    over-relaxation knobs: off, ρ 0.98, 10 plain iterations, interval centre 1 and half-width 1)."""
+    lib = ctypes.CDLL(pdg.api.LIB_PATH)
+    c = pdg.api._Cfg()
+    lib.pd_scene_config_default(ctypes.byref(c))
+    d = pdg.SceneConfig()
+    for name, _ in pdg.api._Cfg._fields_:
+        got = tuple(c.gravity) if name == "gravity" else getattr(c, name)
+        assert got == getattr(d, name), name
+    base = pdg.make_grid(pdg.SceneConfig(grid_nx=6, grid_ny=6))
+    with pytest.raises(pdg.PdError) as e:
+        scene_factor(base, pdg.SceneConfig(cheb_mode=3))
+    assert e.value.code == 1
