@@ -19,6 +19,7 @@ algorithm restated) on all host cores instead. Under torchrun each rank steps it
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import os
 import statistics
@@ -72,6 +73,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-pos-err", action="store_true")
     p.add_argument("--no-fp64-gpu", action="store_true")
+    p.add_argument("--no-cheb", action="store_true")
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
     a = p.parse_args()
@@ -295,6 +297,41 @@ def time_fp64_gpu(P, args, stream, flush, max_steps=10):
             "ctas_per_cloth": sim.info(0)["cluster_ctas"]}
 
 
+def chebyshev_line(P, args, stream, flush, max_steps=100):
+    """The reference's Chebyshev mode (PD_CHEB=1: ρ 0.98 after 10 plain iterations) on the same
+    single-cloth workload and precision: substeps/s timed like `value`, and the last residual after
+    the workload's substeps with and without it (equal iteration budget)."""
+    import torch
+    scenes, cfgs, sub = workload(args.workload, args.batch_count, args.precision)
+    res = {}
+    for mode in (0, 1):
+        cs = [copy.copy(c) for c in cfgs]
+        for c in cs:
+            c.cheb_mode = mode
+        sim = P.Simulator(scenes, cs)
+        sim.set_stream(stream.cuda_stream)
+        if mode == 1:
+            k = min(args.steps, max_steps)
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    sim.step(1, sync=False)
+                    flush.fill_(1.0)
+                for j in range(k):
+                    flush.fill_(float(j))
+                    starts[j].record(stream)
+                    sim.step(1, sync=False)
+                    ends[j].record(stream)
+            torch.cuda.synchronize()
+            ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / k
+            sim = P.Simulator(scenes, cs)
+        sim.step(sub)
+        res[mode] = sim.stats(0)["last_residual"]
+    return {"value": len(scenes) * 1e3 / ms, "unit": UNIT, "steps": k, "rho": 0.98, "plain_iterations": 10,
+            "last_residual": res[1], "last_residual_plain": res[0], "substeps": sub}
+
+
 def time_fp64_one_at_a_time(P, args, budget_s=120.0):
     """Aggregate cloth-substeps/s of the batch run one cloth per launch through the plain FP64
     path: every cloth gets its own simulator, one warm-up and one timed substep (CUDA events);
@@ -464,6 +501,8 @@ def run_ours(args):
                 line["fp64_gpu_batched"] = batched
         if pos_err is not None:
             line["pos_err"] = pos_err
+        if len(scenes) == 1 and not args.no_cheb:
+            line["chebyshev"] = chebyshev_line(P, args, stream, flush)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(scenes, cfgs, sub, args.cpu_sample_seconds)
         print(json.dumps(line), flush=True)
