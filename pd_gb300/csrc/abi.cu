@@ -5,6 +5,7 @@
 #include <chrono>
 #include <iterator>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -1366,17 +1367,34 @@ int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, c
     if (I.cfg.cheb_mode != PD_CHEB_OFF)
       return fail(PD_ERR_UNSUPPORTED, "gradients of over-relaxed iterations (cheb_mode) are not provided");
   if (const int rc_ = s->sync()) return rc_;
-  // device work arrays: per instance [target, force?, checkpoints, iterates, state and adjoints,
-  // per-edge terms, loss]
-  std::vector<size_t> off(count + 1, 0);
-  auto doublesOf = [&](int i) {
+  // device work arrays: per instance [target, force?, every iterate of every substep — or the
+  // (x, v) checkpoints and one substep's iterates —, state and adjoints, per-edge terms, loss].
+  // Every iterate is kept when the batch's copy fits in half of the free device memory and in
+  // PD_GB300_GRADIENT_STORE_BYTES (default 128 GB; 0 always recomputes), which saves the reverse
+  // pass re-running each substep.
+  bool anyGrad = false;
+  for (int i = 0; i < count; ++i)
+    anyGrad = anyGrad || (dkappa && dkappa[i]) || (dv0 && dv0[i]) || (dforce && dforce[i]);
+  auto doublesOf = [&](int i, bool stored) {
     const Instance& I = s->inst[i];
     const size_t n3 = 3 * static_cast<size_t>(I.scene.n), E = I.scene.edges.size();
     const size_t K = static_cast<size_t>(std::max(0, I.cfg.max_iterations));
     const size_t sub = static_cast<size_t>(std::max(1, substeps));
-    return n3 * (2 + 2 * sub + (K + 1) + 8) + 4 * E + 4;  // +4 keeps every instance 32-byte aligned
+    const size_t states = stored ? sub * (K + 1) : 2 * sub + (K + 1);
+    return n3 * (2 + states + 8) + 4 * E + 4;  // +4 keeps every instance 32-byte aligned
   };
-  for (int i = 0; i < count; ++i) off[i + 1] = off[i] + (doublesOf(i) + 3) / 4 * 4;
+  bool stored = false;
+  if (anyGrad) {
+    size_t freeB = 0, totalB = 0;
+    double want = 0.0;
+    for (int i = 0; i < count; ++i) want += 8.0 * doublesOf(i, true);
+    double cap = 128.0 * (1ull << 30);
+    if (const char* e = std::getenv("PD_GB300_GRADIENT_STORE_BYTES")) cap = std::atof(e);
+    if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess)
+      stored = want <= std::min(0.5 * static_cast<double>(freeB), cap);
+  }
+  std::vector<size_t> off(count + 1, 0);
+  for (int i = 0; i < count; ++i) off[i + 1] = off[i] + (doublesOf(i, stored) + 3) / 4 * 4;
   double* dWork = nullptr;
   pdg::GradDev* dG = nullptr;
   PD_CUDA(cudaMalloc(&dWork, sizeof(double) * off[count]));
@@ -1398,12 +1416,19 @@ int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, c
     p += n3;
     g.force = (forces && forces[i]) ? p : nullptr;
     p += n3;
-    g.ckX = p;
-    p += sub * n3;
-    g.ckV = p;
-    p += sub * n3;
-    g.it = p;
-    p += (K + 1) * n3;
+    if (stored) {
+      g.ckX = g.ckV = g.it = nullptr;
+      g.itAll = p;
+      p += sub * (K + 1) * n3;
+    } else {
+      g.itAll = nullptr;
+      g.ckX = p;
+      p += sub * n3;
+      g.ckV = p;
+      p += sub * n3;
+      g.it = p;
+      p += (K + 1) * n3;
+    }
     double** vecs[] = {&g.xs, &g.vs, &g.xb, &g.vb, &g.xkb, &g.xnb, &g.xhb, &g.fb};
     for (double** v : vecs) {
       *v = p;

@@ -14,10 +14,12 @@
 // with pinned vertices at q and λ = 0 on pinned rows (they are identity rows of L). The
 // velocity update v' = (x^K − x_n)·(1 − k_d)/h and the prediction chain the rest.
 //
-// Memory: the forward pass stores (x, v) at the start of every substep (S·48n bytes a cloth);
-// the reverse pass recomputes each substep's K iterates from its checkpoint (K+1 vectors) and
-// walks them backwards. One CTA per cloth runs it all with the FP64 supernodal solve; a batch of
-// problems is one launch.
+// Memory: when HBM allows (S·(K+1)·24n bytes a problem, 130 MB for 64² × 120 substeps × 10
+// iterations) the forward pass stores every iterate and the reverse pass only reads them: 2·S·K
+// solves a gradient. Otherwise the forward pass stores (x, v) at the start of every substep
+// (S·48n bytes) and the reverse pass recomputes each substep's K iterates from its checkpoint:
+// 3·S·K solves. One CTA per cloth runs it all with the FP64 supernodal solve; a batch of problems
+// is one launch.
 #include "device.cuh"
 #include "substep_team.cuh"
 
@@ -103,13 +105,16 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
     G.vs[i] = I.v[i];
   }
   __syncthreads();
+  const size_t itStride = static_cast<size_t>(K + 1) * n3;
   for (int s = 0; s < substeps; ++s) {
-    for (int i = threadIdx.x; i < n3; i += blockDim.x) {
-      G.ckX[(size_t)s * n3 + i] = G.xs[i];
-      G.ckV[(size_t)s * n3 + i] = G.vs[i];
+    if (!G.itAll) {
+      for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+        G.ckX[(size_t)s * n3 + i] = G.xs[i];
+        G.ckV[(size_t)s * n3 + i] = G.vs[i];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    forwardSubstep(J, G, tm, w, t, nullptr);
+    forwardSubstep(J, G, tm, w, t, G.itAll ? G.itAll + s * itStride : nullptr);
   }
   // loss and its gradient w.r.t. the final positions
   double l = 0.0, nfree = 0.0;
@@ -136,12 +141,15 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
   for (int e = threadIdx.x; e < J.ne; e += blockDim.x) G.kb[e] = 0.0;
   __syncthreads();
   for (int s = substeps - 1; s >= 0; --s) {
-    for (int i = threadIdx.x; i < n3; i += blockDim.x) {
-      G.xs[i] = G.ckX[(size_t)s * n3 + i];
-      G.vs[i] = G.ckV[(size_t)s * n3 + i];
+    const double* its = G.itAll ? G.itAll + s * itStride : G.it;  // x^0 .. x^K of substep s
+    if (!G.itAll) {
+      for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+        G.xs[i] = G.ckX[(size_t)s * n3 + i];
+        G.vs[i] = G.ckV[(size_t)s * n3 + i];
+      }
+      __syncthreads();
+      forwardSubstep(J, G, tm, w, t, G.it);
     }
-    __syncthreads();
-    forwardSubstep(J, G, tm, w, t, G.it);  // J.xhat now holds this substep's x̂
     for (int v = threadIdx.x; v < n; v += blockDim.x) {
       const bool p = J.pinned[v] != 0;
       for (int c = 0; c < 3; ++c) {
@@ -166,8 +174,8 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
         const int r = J.iperm[v];
         for (int c = 0; c < 3; ++c) G.xhb[3 * v + c] = fma(mh2, w[3 * r + c], G.xhb[3 * v + c]);
       }
-      const double* xk = G.it + (size_t)k * n3;
-      const double* xk1 = G.it + (size_t)(k + 1) * n3;
+      const double* xk = its + (size_t)k * n3;
+      const double* xk1 = its + (size_t)(k + 1) * n3;
       for (int e = threadIdx.x; e < J.ne; e += blockDim.x) {
         const int a = J.eab[2 * e], b = J.eab[2 * e + 1];
         const bool ap = J.pinned[a] != 0, bp = J.pinned[b] != 0;

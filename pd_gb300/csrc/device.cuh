@@ -172,7 +172,9 @@ struct GradDev {
   const double* force;   // 3n or null
   double* ckX;           // S × 3n checkpoints of x
   double* ckV;           // S × 3n checkpoints of v
-  double* it;            // (K + 1) × 3n iterates of the substep being reversed
+  double* it;            // (K + 1) × 3n iterates of the substep being reversed (recompute mode)
+  double* itAll;         // S × (K + 1) × 3n iterates of every substep, or null: recompute from
+                         // the checkpoints
   double* xs;            // working state
   double* vs;
   double* xb;            // adjoints

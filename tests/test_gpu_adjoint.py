@@ -93,3 +93,21 @@ def test_gradient_batch_equals_single_problems(pdg):
         assert gb[i]["loss"] == g1["loss"]
         for key in ("dkappa", "dv0", "dforce"):
             assert np.array_equal(gb[i][key], g1[key]), (i, key)
+
+
+def test_stored_iterates_equal_recomputed(pdg, monkeypatch):
+    """The reverse pass reads every stored iterate, or recomputes each substep from its checkpoint
+    when the store is capped to zero: the same gradient bit for bit."""
+    scene, cfg, S, targets, force, v0, _ = problem(side=10, substeps=8)
+    out = []
+    for cap in (None, "0"):
+        if cap is None:
+            monkeypatch.delenv("PD_GB300_GRADIENT_STORE_BYTES", raising=False)
+        else:
+            monkeypatch.setenv("PD_GB300_GRADIENT_STORE_BYTES", cap)
+        sim = pdg.Simulator(scene, cfg)
+        sim.set_state(0, scene.positions, v0)
+        out.append(sim.gradient(S, targets, force))
+    assert out[0]["loss"] == out[1]["loss"]
+    for key in ("dkappa", "dv0", "dforce"):
+        assert np.array_equal(out[0][key], out[1][key]), key
