@@ -1452,7 +1452,10 @@ int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, c
                                      s->stream) != cudaSuccess)
     rc = cudaFail(cudaGetLastError(), "gradient descriptors");
   if (rc == PD_OK) {
-    const int lrc = pdg::launchGradient(s->dDesc, dG, count, substeps, smem, s->stream);
+    // a cluster per problem where the FP64 path runs clusters (the planner's CTAs per cloth)
+    int cs = supernodalFp64(s->precision()) ? s->teamCtas : 1;
+    if (cs > 1 && pdg::gradClusterSupported(cs) != cs) cs = 1;
+    const int lrc = pdg::launchGradient(s->dDesc, dG, count, cs, substeps, smem, s->stream);
     if (lrc != 0) rc = cudaFail(static_cast<cudaError_t>(lrc), "gradient launch");
   }
   for (int i = 0; i < count && rc == PD_OK; ++i) {

@@ -18,8 +18,9 @@
 // iterations) the forward pass stores every iterate and the reverse pass only reads them: 2·S·K
 // solves a gradient. Otherwise the forward pass stores (x, v) at the start of every substep
 // (S·48n bytes) and the reverse pass recomputes each substep's K iterates from its checkpoint:
-// 3·S·K solves. One CTA per cloth runs it all with the FP64 supernodal solve; a batch of problems
-// is one launch.
+// 3·S·K solves. A problem is run by one CTA or by a thread-block cluster (the FP64 supernodal
+// solve strided over the cluster, vectors in L2, sums through distributed shared memory); a batch
+// of problems is one launch.
 #include "device.cuh"
 #include "substep_team.cuh"
 
@@ -37,17 +38,35 @@ __device__ __forceinline__ double blockSum(double v, double* red) {
   return s;
 }
 
+// Sum over the team (CTA sums added in rank order, so every CTA gets the same bits). `slots` is
+// a 2-entry shared array used alternately, as in teamMax.
+template <bool CLUSTER>
+__device__ __forceinline__ double teamSum(const Team<CLUSTER>& tm, double v, double* red, double* slots,
+                                          int& parity) {
+  v = blockSum(v, red);
+  if (!CLUSTER) return v;
+  double* slot = slots + parity;
+  parity ^= 1;
+  if (threadIdx.x == 0) *slot = v;
+  cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+  cl.sync();
+  double s = 0.0;
+  for (int r = 0; r < tm.size; ++r) s += *cl.map_shared_rank(slot, r);
+  return s;
+}
+
 // One substep of the differentiable map from (J.x, J.v) in place; it[k] receives x^k if given.
-__device__ void forwardSubstep(const InstanceDev& J, const GradDev& G, const Team<false>& tm, double* w, double* t,
+template <bool CLUSTER>
+__device__ void forwardSubstep(const InstanceDev& J, const GradDev& G, const Team<CLUSTER>& tm, double* w, double* t,
                                double* it) {
-  const int n = J.n;
+  const int n = J.n, T = tm.tid(), NT = tm.count();
   const double h2 = J.h * J.h;
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {  // predict with the external force
+  for (int v = T; v < n; v += NT) {  // predict with the external force
     const double m = J.m[v];
     const double mh2 = m * J.invH2;
     for (int c = 0; c < 3; ++c) {
-      const double p = J.x[3 * v + c];
-      double xh = (p + J.v[3 * v + c] * J.h) + J.gh2[c];
+      const double p = tm.ld(J.x + 3 * v + c);
+      double xh = (p + tm.ld(J.v + 3 * v + c) * J.h) + J.gh2[c];
       if (G.force && m > 0.0) xh = fma(G.force[3 * v + c], h2 / m, xh);
       J.xn[3 * v + c] = p;
       J.xhat[3 * v + c] = xh;
@@ -55,102 +74,100 @@ __device__ void forwardSubstep(const InstanceDev& J, const GradDev& G, const Tea
       if (it) it[3 * v + c] = p;
     }
   }
-  for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, J.x, e, false);
-  __syncthreads();
+  tm.sync();
+  for (int e = T; e < J.ne; e += NT) edgeTerms(J, tm, J.x, e, false);
+  tm.sync();
   for (int k = 0; k < J.maxIter; ++k) {
-    for (int v = threadIdx.x; v < n; v += blockDim.x) gatherRow(J, tm, v, w);
-    __syncthreads();
-    TeamSolve<false>::run(J, tm, w, t);
-    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    for (int v = T; v < n; v += NT) gatherRow(J, tm, v, w);
+    tm.sync();
+    TeamSolve<CLUSTER>::run(J, tm, w, t);
+    for (int v = T; v < n; v += NT) {
       const int r = J.iperm[v];
       for (int c = 0; c < 3; ++c) {
-        J.x[3 * v + c] = w[3 * r + c];
-        if (it) it[(size_t)(k + 1) * 3 * n + 3 * v + c] = w[3 * r + c];
+        const double x = tm.ld(w + 3 * r + c);
+        J.x[3 * v + c] = x;
+        if (it) it[(size_t)(k + 1) * 3 * n + 3 * v + c] = x;
       }
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < J.ne; e += blockDim.x) edgeTerms(J, tm, J.x, e, false);
-    __syncthreads();
+    tm.sync();
+    for (int e = T; e < J.ne; e += NT) edgeTerms(J, tm, J.x, e, false);
+    tm.sync();
   }
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {  // velocity, damping, pin resnap
+  for (int v = T; v < n; v += NT) {  // velocity, damping, pin resnap
     for (int c = 0; c < 3; ++c) {
       if (J.pinned[v]) {
         J.v[3 * v + c] = 0.0;
         J.x[3 * v + c] = J.q[3 * v + c];
       } else {
-        J.v[3 * v + c] = (J.x[3 * v + c] - J.xn[3 * v + c]) * J.dampInvH;
+        J.v[3 * v + c] = (tm.ld(J.x + 3 * v + c) - tm.ld(J.xn + 3 * v + c)) * J.dampInvH;
       }
     }
   }
-  __syncthreads();
+  tm.sync();
 }
 
-__global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDev* __restrict__ insts,
-                                                               const GradDev* __restrict__ grads, int substeps,
-                                                               int smemBytes) {
-  extern __shared__ double smem[];
-  __shared__ double red[32];
-  const GradDev& G = grads[blockIdx.x];
-  InstanceDev J = insts[blockIdx.x];  // the instance with its state redirected to the work arrays
+// Loss and gradients of one problem by a team; w, t: the solve's vectors (shared memory for one
+// CTA, the instance's L2 workspaces for a cluster).
+template <bool CLUSTER>
+__device__ void gradientOf(const InstanceDev& I, const GradDev& G, const Team<CLUSTER>& tm, int substeps, double* w,
+                           double* t, double* red, double* slots) {
+  InstanceDev J = I;  // the instance with its state redirected to the work arrays
   J.x = G.xs;
   J.v = G.vs;
   const int n = J.n, n3 = 3 * n, K = J.maxIter;
-  const bool inSmem = 6 * n * static_cast<int>(sizeof(double)) <= smemBytes;
-  double* w = inSmem ? smem : J.w;
-  double* t = inSmem ? smem + n3 : J.tbuf;
-  const Team<false> tm{0, 1};
-  const InstanceDev& I = insts[blockIdx.x];
-  for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+  const int T = tm.tid(), NT = tm.count();
+  int parity = 0;
+  for (int i = T; i < n3; i += NT) {
     G.xs[i] = I.x[i];
     G.vs[i] = I.v[i];
   }
-  __syncthreads();
+  tm.sync();
   const size_t itStride = static_cast<size_t>(K + 1) * n3;
   for (int s = 0; s < substeps; ++s) {
     if (!G.itAll) {
-      for (int i = threadIdx.x; i < n3; i += blockDim.x) {
-        G.ckX[(size_t)s * n3 + i] = G.xs[i];
-        G.ckV[(size_t)s * n3 + i] = G.vs[i];
+      for (int i = T; i < n3; i += NT) {
+        G.ckX[(size_t)s * n3 + i] = tm.ld(G.xs + i);
+        G.ckV[(size_t)s * n3 + i] = tm.ld(G.vs + i);
       }
-      __syncthreads();
+      tm.sync();
     }
     forwardSubstep(J, G, tm, w, t, G.itAll ? G.itAll + s * itStride : nullptr);
   }
   // loss and its gradient w.r.t. the final positions
   double l = 0.0, nfree = 0.0;
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {
+  for (int v = T; v < n; v += NT) {
     if (J.pinned[v]) continue;
     nfree += 1.0;
     for (int c = 0; c < 3; ++c) {
-      const double d = G.xs[3 * v + c] - G.target[3 * v + c];
+      const double d = tm.ld(G.xs + 3 * v + c) - G.target[3 * v + c];
       l = fma(d, d, l);
     }
   }
-  l = blockSum(l, red);
-  nfree = blockSum(nfree, red);
-  if (threadIdx.x == 0) *G.loss = nfree > 0.0 ? l / nfree : 0.0;
+  l = teamSum(tm, l, red, slots, parity);
+  nfree = teamSum(tm, nfree, red, slots, parity);
+  if (T == 0) *G.loss = nfree > 0.0 ? l / nfree : 0.0;
   if (!G.wantGrad) return;
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {
+  for (int v = T; v < n; v += NT) {
     for (int c = 0; c < 3; ++c) {
       const int i = 3 * v + c;
-      G.xb[i] = J.pinned[v] ? 0.0 : 2.0 * (G.xs[i] - G.target[i]) / nfree;
+      G.xb[i] = J.pinned[v] ? 0.0 : 2.0 * (tm.ld(G.xs + i) - G.target[i]) / nfree;
       G.vb[i] = 0.0;
       G.fb[i] = 0.0;
     }
   }
-  for (int e = threadIdx.x; e < J.ne; e += blockDim.x) G.kb[e] = 0.0;
-  __syncthreads();
+  for (int e = T; e < J.ne; e += NT) G.kb[e] = 0.0;
+  tm.sync();
   for (int s = substeps - 1; s >= 0; --s) {
     const double* its = G.itAll ? G.itAll + s * itStride : G.it;  // x^0 .. x^K of substep s
     if (!G.itAll) {
-      for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+      for (int i = T; i < n3; i += NT) {
         G.xs[i] = G.ckX[(size_t)s * n3 + i];
         G.vs[i] = G.ckV[(size_t)s * n3 + i];
       }
-      __syncthreads();
+      tm.sync();
       forwardSubstep(J, G, tm, w, t, G.it);
     }
-    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    for (int v = T; v < n; v += NT) {
       const bool p = J.pinned[v] != 0;
       for (int c = 0; c < 3; ++c) {
         const int i = 3 * v + c;
@@ -159,33 +176,34 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
         G.xhb[i] = 0.0;
       }
     }
-    __syncthreads();
+    tm.sync();
     for (int k = K - 1; k >= 0; --k) {
       // λ = L⁻¹·x̄^{k+1} (pinned rows zero), in elimination order in w
-      for (int v = threadIdx.x; v < n; v += blockDim.x) {
+      for (int v = T; v < n; v += NT) {
         const int r = J.iperm[v];
         for (int c = 0; c < 3; ++c) w[3 * r + c] = G.xkb[3 * v + c];
       }
-      __syncthreads();
-      TeamSolve<false>::run(J, tm, w, t);
-      for (int v = threadIdx.x; v < n; v += blockDim.x) {
+      tm.sync();
+      TeamSolve<CLUSTER>::run(J, tm, w, t);
+      for (int v = T; v < n; v += NT) {
         if (J.pinned[v]) continue;
         const double mh2 = J.m[v] * J.invH2;
         const int r = J.iperm[v];
-        for (int c = 0; c < 3; ++c) G.xhb[3 * v + c] = fma(mh2, w[3 * r + c], G.xhb[3 * v + c]);
+        for (int c = 0; c < 3; ++c) G.xhb[3 * v + c] = fma(mh2, tm.ld(w + 3 * r + c), G.xhb[3 * v + c]);
       }
       const double* xk = its + (size_t)k * n3;
       const double* xk1 = its + (size_t)(k + 1) * n3;
-      for (int e = threadIdx.x; e < J.ne; e += blockDim.x) {
+      for (int e = T; e < J.ne; e += NT) {
         const int a = J.eab[2 * e], b = J.eab[2 * e + 1];
         const bool ap = J.pinned[a] != 0, bp = J.pinned[b] != 0;
         double g0 = 0.0, g1 = 0.0, g2 = 0.0, kbe = 0.0;
         if (!(ap && bp)) {
           const int ra = J.iperm[a], rb = J.iperm[b];
-          const double l0 = (ap ? 0.0 : w[3 * ra]) - (bp ? 0.0 : w[3 * rb]);
-          const double l1 = (ap ? 0.0 : w[3 * ra + 1]) - (bp ? 0.0 : w[3 * rb + 1]);
-          const double l2 = (ap ? 0.0 : w[3 * ra + 2]) - (bp ? 0.0 : w[3 * rb + 2]);
-          const double r0 = xk[3 * a] - xk[3 * b], r1 = xk[3 * a + 1] - xk[3 * b + 1], r2 = xk[3 * a + 2] - xk[3 * b + 2];
+          const double l0 = (ap ? 0.0 : tm.ld(w + 3 * ra)) - (bp ? 0.0 : tm.ld(w + 3 * rb));
+          const double l1 = (ap ? 0.0 : tm.ld(w + 3 * ra + 1)) - (bp ? 0.0 : tm.ld(w + 3 * rb + 1));
+          const double l2 = (ap ? 0.0 : tm.ld(w + 3 * ra + 2)) - (bp ? 0.0 : tm.ld(w + 3 * rb + 2));
+          const double r0 = tm.ld(xk + 3 * a) - tm.ld(xk + 3 * b), r1 = tm.ld(xk + 3 * a + 1) - tm.ld(xk + 3 * b + 1),
+                       r2 = tm.ld(xk + 3 * a + 2) - tm.ld(xk + 3 * b + 2);
           const double len = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
           double d0 = 0.0, d1 = 0.0, d2 = 0.0;
           if (!(len <= 1e-12)) {
@@ -200,8 +218,8 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
             g1 = ks * (l1 - u1 * ul);
             g2 = ks * (l2 - u2 * ul);
           }
-          const double q0 = xk1[3 * a] - xk1[3 * b], q1 = xk1[3 * a + 1] - xk1[3 * b + 1],
-                       q2 = xk1[3 * a + 2] - xk1[3 * b + 2];
+          const double q0 = tm.ld(xk1 + 3 * a) - tm.ld(xk1 + 3 * b), q1 = tm.ld(xk1 + 3 * a + 1) - tm.ld(xk1 + 3 * b + 1),
+                       q2 = tm.ld(xk1 + 3 * a + 2) - tm.ld(xk1 + 3 * b + 2);
           kbe = l0 * (d0 - q0) + l1 * (d1 - q1) + l2 * (d2 - q2);
         }
         G.kb[e] += kbe;
@@ -209,28 +227,28 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
         G.ge[3 * e + 1] = g1;
         G.ge[3 * e + 2] = g2;
       }
-      __syncthreads();
-      for (int v = threadIdx.x; v < n; v += blockDim.x) {  // x̄^k, gathered per vertex
+      tm.sync();
+      for (int v = T; v < n; v += NT) {  // x̄^k, gathered per vertex
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         if (!J.pinned[v]) {
           for (int q = J.rstart[v]; q < J.rstart[v + 1]; ++q) {
             const int p = J.rinc[q];
             const int e = p >> 1;
             const double sg = (p & 1) ? -1.0 : 1.0;
-            a0 = fma(sg, G.ge[3 * e], a0);
-            a1 = fma(sg, G.ge[3 * e + 1], a1);
-            a2 = fma(sg, G.ge[3 * e + 2], a2);
+            a0 = fma(sg, tm.ld(G.ge + 3 * e), a0);
+            a1 = fma(sg, tm.ld(G.ge + 3 * e + 1), a1);
+            a2 = fma(sg, tm.ld(G.ge + 3 * e + 2), a2);
           }
         }
         G.xkb[3 * v] = a0;
         G.xkb[3 * v + 1] = a1;
         G.xkb[3 * v + 2] = a2;
       }
-      __syncthreads();
+      tm.sync();
     }
     // x^0 = x_n and x̂ = x_n + h·v_n + h²·g + h²·f/m
     const double h2 = J.h * J.h;
-    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    for (int v = T; v < n; v += NT) {
       const bool p = J.pinned[v] != 0;
       const double m = J.m[v];
       for (int c = 0; c < 3; ++c) {
@@ -244,14 +262,78 @@ __global__ void __launch_bounds__(kBlockThreads) gradientKernel(const InstanceDe
         if (m > 0.0) G.fb[i] = fma(h2 / m, G.xhb[i], G.fb[i]);
       }
     }
-    __syncthreads();
+    tm.sync();
   }
+}
+
+__global__ void __launch_bounds__(kBlockThreads, 1) gradientKernel(const InstanceDev* __restrict__ insts,
+                                                               const GradDev* __restrict__ grads, int substeps,
+                                                               int smemBytes) {
+  extern __shared__ double smem[];
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  const InstanceDev& I = insts[blockIdx.x];
+  const bool inSmem = 6 * I.n * static_cast<int>(sizeof(double)) <= smemBytes;
+  double* w = inSmem ? smem : I.w;
+  double* t = inSmem ? smem + 3 * I.n : I.tbuf;
+  const Team<false> tm{0, 1};
+  gradientOf<false>(I, grads[blockIdx.x], tm, substeps, w, t, red, slots);
+}
+
+__global__ void __launch_bounds__(kBlockThreads, 1) gradientClusterKernel(const InstanceDev* __restrict__ insts,
+                                                                      const GradDev* __restrict__ grads,
+                                                                      int substeps) {
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+  const int cs = static_cast<int>(cl.num_blocks());
+  const int p = static_cast<int>(blockIdx.x) / cs;
+  const InstanceDev& I = insts[p];
+  const Team<true> tm{static_cast<int>(cl.block_rank()), cs};
+  gradientOf<true>(I, grads[p], tm, substeps, I.w, I.tbuf, red, slots);
+}
+
+cudaLaunchConfig_t gradClusterConfig(int blocks, int clusterSize, void* stream, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = clusterSize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
 }
 
 }  // namespace
 
-int launchGradient(const InstanceDev* d, const GradDev* g, int count, int substeps, int smemBytes, void* stream) {
+int gradClusterSupported(int want) {
+  static int cached[17] = {0};
+  if (want < 2 || want > 16) return 0;
+  if (cached[want]) return cached[want] > 0 ? want : 0;
+  if (want > 8) cudaFuncSetAttribute(gradientClusterKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = gradClusterConfig(want, want, nullptr, attr);
+  int clusters = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, gradientClusterKernel, &cfg);
+  if (e != cudaSuccess) cudaGetLastError();
+  cached[want] = (e == cudaSuccess && clusters > 0) ? 1 : -1;
+  return cached[want] > 0 ? want : 0;
+}
+
+int launchGradient(const InstanceDev* d, const GradDev* g, int count, int clusterSize, int substeps, int smemBytes,
+                   void* stream) {
   if (count <= 0) return 0;
+  if (clusterSize > 1) {
+    if (gradClusterSupported(clusterSize) != clusterSize) return static_cast<int>(cudaErrorInvalidConfiguration);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = gradClusterConfig(count * clusterSize, clusterSize, stream, attr);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, gradientClusterKernel, d, g, substeps);
+    return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
+  }
   static bool attrSet = false;
   if (!attrSet) {
     cudaFuncSetAttribute(gradientKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

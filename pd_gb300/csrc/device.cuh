@@ -189,9 +189,11 @@ struct GradDev {
   int32_t wantGrad;
 };
 // Loss (and, where wantGrad, gradients) of `count` problems, one CTA each (smemBytes: 48·n when
-// the solve vectors fit).
-int launchGradient(const InstanceDev* dInstances, const GradDev* dGrads, int count, int substeps, int smemBytes,
-                   void* stream);
+// the solve vectors fit) or a thread-block cluster of clusterSize CTAs each (vectors in the
+// instances' L2 workspaces). gradClusterSupported: clusterSize if the device runs it, else 0.
+int launchGradient(const InstanceDev* dInstances, const GradDev* dGrads, int count, int clusterSize, int substeps,
+                   int smemBytes, void* stream);
+int gradClusterSupported(int clusterSize);
 
 constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per
