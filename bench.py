@@ -76,6 +76,8 @@ def parse():
     p.add_argument("--no-cheb", action="store_true")
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
+    p.add_argument("--grad-side", type=int, default=64)         # smaller only for profiling captures
+    p.add_argument("--grad-substeps", type=int, default=120)
     a = p.parse_args()
     if a.steps is None:
         a.steps = 3 if a.workload == "differentiable" else 600
@@ -512,16 +514,16 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------------------- gradients (C5)
-def grad_problems(count):
-    """`count` differentiable problems on one 64×64 cloth: hidden stiffness κ* from seeds 1..count,
-    targets = final positions of an FP64 run with κ*; parameters at κ = 2300, v0 = 0, f = 0."""
-    import copy
+def grad_problems(count, side=64, substeps=120):
+    """`count` differentiable problems on one side×side cloth (64×64, 120 substeps: the workload;
+    smaller only for profiling captures): hidden stiffness κ* from seeds 1..count, targets = final
+    positions of an FP64 run with κ*; parameters at κ = 2300, v0 = 0, f = 0."""
     import pd_gb300 as P
     from pd_gb300 import workloads as W
-    scene, cfg, S, _ = W.differentiable()
+    scene, cfg, S, _ = W.differentiable(side=side, substeps=substeps)
     cfg = copy.copy(cfg)
     cfg.precision = PRECISIONS["fp64"][0]
-    kstars = [W.differentiable(seed=s + 1)[3] for s in range(count)]
+    kstars = [W.differentiable(side=side, substeps=substeps, seed=s + 1)[3] for s in range(count)]
     ref = P.Simulator([scene] * count, [cfg] * count)
     for i, k in enumerate(kstars):
         ref.set_edge_stiffness(k, i)
@@ -575,7 +577,7 @@ def run_gradients(args):
         return 0
     torch.cuda.set_device(local)
     count = args.grad_batch
-    scene, cfg, S, targets = grad_problems(count)
+    scene, cfg, S, targets = grad_problems(count, args.grad_side, args.grad_substeps)
     zero = np.zeros((scene.n, 3))
     sim = P.Simulator([scene] * count, [cfg] * count)
     for _ in range(args.warmup):
@@ -625,6 +627,13 @@ def run_gradients(args):
            for k in ("dkappa", "dv0", "dforce")}
     info = sim.info(0)
     n3 = 3 * scene.n
+    # roofline: a gradient runs the S·K forward iterations and S·K adjoint solves, each at least as
+    # much traffic as a FP64 substep's iteration (algorithmic_bytes), over the measured launch time
+    F = info["factor_nnz"]
+    per_launch = count * 2 * S * algorithmic_bytes(scene, F, cfg.max_iterations, "fp64")
+    peak, peak_kind = read_peaks()
+    achieved = per_launch / (dt / args.steps) / 1e9
+    fp64_gops = count * 2 * S * fp64_ops(scene, F, cfg.max_iterations) / (dt / args.steps) / 1e9
     line = {"metric": METRIC, "value": value, "unit": "grads/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -638,6 +647,11 @@ def run_gradients(args):
             "gpu_launches": args.steps,
             "e2e": {"value": value, "unit": "grads/s", "h2d_bytes_per_step": count * 2 * 8 * n3,
                     "d2h_bytes_per_step": count * (8 * (2 * n3 + scene.edges.shape[0]) + 8)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "gradientClusterKernel" if info["cluster_ctas"] > 1 else "gradientKernel",
+                         "algorithmic_bytes_per_launch": per_launch},
+            "fp64": {"achieved_gops": fp64_gops, "peak_gops": 503.4, "frac": fp64_gops / 503.4},
             "grad_check": {"fd_directions": len(dirs), **fd_err, "vs_cpu_reference_rel": rel,
                            "loss_problem0": g0["loss"], "loss_cpu_reference": r["loss"]},
             "clocks": clocks,
