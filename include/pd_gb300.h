@@ -127,6 +127,18 @@ int pd_make_grid(const pd_scene_config* cfg, double* positions, double* masses, 
                  int32_t* edges, double* edge_rest, double* edge_stiffness, int32_t* bends,
                  double* bend_stiffness);
 
+/* ---- Triangle meshes from the text of an OBJ file: Mesh::loadObj + makeScene (core/mesh/
+ *      Mesh.cpp:56-153, core/sim/Scene.cpp:44-64). "v x y z" vertices; the first three corner
+ *      indices of each "f" line ("a", "a/b", "a/b/c", "a//c", 1-based); distance constraints are the
+ *      triangles' unique edges in first-seen order at cfg->stiffness; masses cfg->density·area/3 per
+ *      triangle corner; no shear, bend or pins (set pins in the returned flags). A file the
+ *      reference could not load, or whose indices it would read out of range, is
+ *      PD_ERR_INVALID_ARGUMENT (the reference falls back to a grid). Call pd_obj_counts to size the
+ *      arrays. ---- */
+int pd_obj_counts(const char* obj_text, int32_t* n_vertices, int32_t* n_edges);
+int pd_make_obj(const pd_scene_config* cfg, const char* obj_text, double* positions, double* masses, uint8_t* pinned,
+                int32_t* edges, double* edge_rest, double* edge_stiffness);
+
 /* ---- Global solver: IGlobalSolver (core/solver/IGlobalSolver.h:45-127) ---- */
 typedef struct pd_solver pd_solver;
 

@@ -76,6 +76,10 @@ def lib():
     L.oracle_grid_counts.argtypes = [_P(_GridSpec), _P(C.c_int), _P(C.c_int), _P(C.c_int)]
     L.oracle_make_grid.argtypes = [_P(_GridSpec), dp, dp, u8p, ip, dp, dp, ip, dp]
     L.oracle_make_grid.restype = C.c_int
+    L.oracle_obj_counts.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int)]
+    L.oracle_obj_counts.restype = C.c_int
+    L.oracle_make_obj.argtypes = [C.c_char_p, C.c_double, C.c_double, dp, dp, u8p, ip, dp, dp]
+    L.oracle_make_obj.restype = C.c_int
     L.oracle_sim_create.argtypes = [C.c_int, dp, dp, dp, u8p, dp, C.c_int, ip, dp, dp, C.c_int, ip, dp,
                                     _P(_Config), ip]
     L.oracle_sim_create.restype = C.c_void_p
@@ -207,6 +211,25 @@ def make_grid(spec: GridSpec) -> Mesh:
     if rc != 0:
         raise ValueError("invalid grid spec")
     return Mesh(pos, mass, pinned, eab, er, ek, babc, bk)
+
+
+def make_obj(text: str, stiffness: float = 2.3e3, density: float = 1.0) -> Mesh:
+    """The OBJ triangle mesh of ``makeScene`` (Mesh::loadObj + surface masses)."""
+    L = lib()
+    raw = text.encode()
+    nv, ne = C.c_int(), C.c_int()
+    if L.oracle_obj_counts(raw, C.byref(nv), C.byref(ne)) != 0:
+        raise ValueError("OBJ text the reference cannot load")
+    nv, ne = nv.value, ne.value
+    pos = np.zeros((nv, 3))
+    mass = np.zeros(nv)
+    pinned = np.zeros(nv, np.uint8)
+    eab = np.zeros((ne, 2), np.int32)
+    er = np.zeros(ne)
+    ek = np.zeros(ne)
+    L.oracle_make_obj(raw, stiffness, density, _ptr(pos, C.c_double), _ptr(mass, C.c_double),
+                      _ptr(pinned, C.c_uint8), _ptr(eab, C.c_int32), _ptr(er, C.c_double), _ptr(ek, C.c_double))
+    return Mesh(pos, mass, pinned, eab, er, ek)
 
 
 class OracleSim:

@@ -8,6 +8,10 @@
 #include "pd_oracle.h"
 
 #include <algorithm>
+#include <unordered_set>
+#include <string>
+#include <sstream>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -819,6 +823,116 @@ int stepOnce(oracle_sim& s) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------- OBJ meshes
+namespace {
+
+struct ObjMesh {
+  std::vector<V3> verts;
+  std::vector<std::array<int, 3>> tris;
+  std::vector<int> ea, eb;
+  std::vector<double> rest, mass;
+};
+
+// Mesh::loadObj (core/mesh/Mesh.cpp:56-127): "v" lines read three numbers, "f" lines the integer
+// before the first '/' of up to three tokens (1-based); a face with fewer than three is dropped, a
+// token that is not a number fails the load. Indices outside the vertex list also fail here (the
+// reference would read out of range). Edges: each triangle's (t0,t1), (t1,t2), (t2,t0) in order,
+// skipping a == b and pairs already seen.
+bool parseObj(const char* text, double density, ObjMesh& out) {
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ss(line);
+    std::string tag;
+    ss >> tag;
+    if (tag == "v") {
+      double x = 0, y = 0, z = 0;
+      ss >> x >> y >> z;
+      out.verts.push_back(V3{x, y, z});
+    } else if (tag == "f") {
+      std::array<int, 3> idx{};
+      int count = 0;
+      std::string token;
+      while (count < 3 && ss >> token) {
+        const std::size_t slash = token.find('/');
+        const std::string first = slash == std::string::npos ? token : token.substr(0, slash);
+        try {
+          idx[count] = std::stoi(first) - 1;
+        } catch (...) {
+          return false;
+        }
+        ++count;
+      }
+      if (count == 3) out.tris.push_back(idx);
+    }
+  }
+  const int n = static_cast<int>(out.verts.size());
+  if (n == 0 || out.tris.empty()) return false;
+  for (const auto& t : out.tris)
+    for (int k = 0; k < 3; ++k)
+      if (t[k] < 0 || t[k] >= n) return false;
+  std::unordered_set<uint64_t> seen;
+  for (const auto& t : out.tris) {
+    for (int k = 0; k < 3; ++k) {
+      const int a = t[k], b = t[(k + 1) % 3];
+      if (a == b) continue;
+      const uint64_t key = (static_cast<uint64_t>(static_cast<uint32_t>(std::min(a, b))) << 32) |
+                           static_cast<uint32_t>(std::max(a, b));
+      if (!seen.insert(key).second) continue;
+      out.ea.push_back(a);
+      out.eb.push_back(b);
+      out.rest.push_back(length(sub(out.verts[b], out.verts[a])));
+    }
+  }
+  // Mesh::computeMassesFromSurfaces (Mesh.cpp:129-153) with makeScene's density
+  out.mass.assign(n, 0.0);
+  const double rho = density > 0.0 ? density : 1.0;
+  for (const auto& t : out.tris) {
+    const V3 p0 = out.verts[t[0]], p1 = out.verts[t[1]], p2 = out.verts[t[2]];
+    const V3 u = sub(p1, p0), w = sub(p2, p0);
+    const V3 c{u.y * w.z - u.z * w.y, u.z * w.x - u.x * w.z, u.x * w.y - u.y * w.x};
+    const double area = 0.5 * length(c);
+    for (int k = 0; k < 3; ++k) out.mass[t[k]] += rho * area / 3.0;
+  }
+  double minPositive = 1e300;
+  for (double m : out.mass)
+    if (m > 1e-12) minPositive = std::min(minPositive, m);
+  if (minPositive > 1e299) minPositive = 1.0;
+  for (double& m : out.mass)
+    if (m < 1e-12) m = minPositive;
+  return true;
+}
+
+}  // namespace
+
+extern "C" int oracle_obj_counts(const char* text, int* nv, int* ne) {
+  ObjMesh m;
+  if (!text || !parseObj(text, 1.0, m)) return -1;
+  *nv = static_cast<int>(m.verts.size());
+  *ne = static_cast<int>(m.ea.size());
+  return 0;
+}
+
+extern "C" int oracle_make_obj(const char* text, double stiffness, double density, double* pos, double* mass,
+                               uint8_t* pinned, int* edges, double* rest, double* k) {
+  ObjMesh m;
+  if (!text || !parseObj(text, density, m)) return -1;
+  for (size_t v = 0; v < m.verts.size(); ++v) {
+    pos[3 * v] = m.verts[v].x;
+    pos[3 * v + 1] = m.verts[v].y;
+    pos[3 * v + 2] = m.verts[v].z;
+    mass[v] = m.mass[v];
+    pinned[v] = 0;
+  }
+  for (size_t e = 0; e < m.ea.size(); ++e) {
+    edges[2 * e] = m.ea[e];
+    edges[2 * e + 1] = m.eb[e];
+    rest[e] = m.rest[e];
+    k[e] = stiffness;
+  }
+  return 0;
+}
 
 // ---------------------------------------------------------------------- grid generation
 extern "C" void oracle_grid_counts(const oracle_grid_spec* g, int* nv, int* ne, int* nb) {

@@ -66,6 +66,13 @@ typedef struct oracle_grid_spec {
                              2 = whole row ny-1, 3 = corner (0, ny-1) only, 4 = none */
 } oracle_grid_spec;
 
+/* Triangle mesh from OBJ text (restates Mesh::loadObj and Mesh::computeMassesFromSurfaces,
+ * core/mesh/Mesh.cpp:56-153, as makeScene applies them, core/sim/Scene.cpp:44-64). Returns 0, or
+ * -1 where the reference's loader fails or would index out of range. */
+int oracle_obj_counts(const char* text, int* n_vertices, int* n_edges);
+int oracle_make_obj(const char* text, double stiffness, double density, double* positions, double* masses,
+                    uint8_t* pinned, int* edges, double* edge_rest, double* edge_k);
+
 /* Counts of a grid scene, so callers can size the arrays of oracle_make_grid. */
 void oracle_grid_counts(const oracle_grid_spec* spec, int* n_vertices, int* n_edges, int* n_bends);
 

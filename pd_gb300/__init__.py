@@ -26,4 +26,5 @@ from .api import (  # noqa: F401
     GpuDirectSolver,
     load_library,
     make_grid,
+    make_obj,
 )

@@ -102,6 +102,8 @@ _SIGS = {
     "pd_scene_config_default": ([C.POINTER(_Cfg)], None),
     "pd_grid_counts": ([C.POINTER(_Cfg), _ip, _ip, _ip], C.c_int),
     "pd_make_grid": ([C.POINTER(_Cfg), _dp, _dp, _u8p, _ip, _dp, _dp, _ip, _dp], C.c_int),
+    "pd_obj_counts": ([C.c_char_p, _ip, _ip], C.c_int),
+    "pd_make_obj": ([C.POINTER(_Cfg), C.c_char_p, _dp, _dp, _u8p, _ip, _dp, _dp], C.c_int),
     "pd_solver_create": ([C.POINTER(C.c_void_p)], C.c_int),
     "pd_solver_destroy": ([C.c_void_p], C.c_int),
     "pd_solver_analyze": ([C.c_void_p, C.c_int32, _ip, _ip], C.c_int),
@@ -299,6 +301,30 @@ def make_grid(cfg: SceneConfig) -> GridScene:
                             _ptr(e, C.c_int32), _ptr(er, C.c_double), _ptr(ek, C.c_double),
                             _ptr(b, C.c_int32), _ptr(bk, C.c_double)))
     return GridScene(pos, mass, pin, e, er, ek, b, bk)
+
+
+def make_obj(obj, cfg: SceneConfig) -> GridScene:
+    """The triangle mesh of ``makeScene`` with a mesh path (``Mesh::loadObj`` + surface masses,
+    core/mesh/Mesh.cpp:56-153), built by the library (pd_make_obj). ``obj`` is the path of an OBJ
+    file or its text; cfg supplies stiffness and density. No pins: set ``scene.pinned``."""
+    lib = load_library()
+    if "\n" not in obj and os.path.exists(obj):
+        with open(obj) as f:
+            obj = f.read()
+    text = obj.encode()
+    c = cfg.c()
+    nv, ne = C.c_int32(), C.c_int32()
+    _check(lib.pd_obj_counts(text, C.byref(nv), C.byref(ne)))
+    nv, ne = nv.value, ne.value
+    pos = np.zeros((nv, 3))
+    mass = np.zeros(nv)
+    pin = np.zeros(nv, np.uint8)
+    e = np.zeros((ne, 2), np.int32)
+    er = np.zeros(ne)
+    ek = np.zeros(ne)
+    _check(lib.pd_make_obj(C.byref(c), text, _ptr(pos, C.c_double), _ptr(mass, C.c_double), _ptr(pin, C.c_uint8),
+                           _ptr(e, C.c_int32), _ptr(er, C.c_double), _ptr(ek, C.c_double)))
+    return GridScene(pos, mass, pin, e, er, ek)
 
 
 class Simulator:

@@ -1009,6 +1009,35 @@ int pd_make_grid(const pd_scene_config* cfg, double* pos, double* mass, uint8_t*
   return PD_OK;
 }
 
+int pd_obj_counts(const char* obj_text, int32_t* n_vertices, int32_t* n_edges) {
+  if (!obj_text || !n_vertices || !n_edges) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  pdg::Scene s;
+  std::string err;
+  if (!pdg::makeObj(obj_text, 1.0, 1.0, s, &err)) return fail(PD_ERR_INVALID_ARGUMENT, "OBJ: " + err);
+  *n_vertices = s.n;
+  *n_edges = static_cast<int32_t>(s.edges.size());
+  return PD_OK;
+}
+
+int pd_make_obj(const pd_scene_config* cfg, const char* obj_text, double* pos, double* mass, uint8_t* pinned,
+                int32_t* edges, double* rest, double* k) {
+  if (!cfg || !obj_text || !pos || !mass || !pinned || !edges || !rest || !k)
+    return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  pdg::Scene s;
+  std::string err;
+  if (!pdg::makeObj(obj_text, cfg->stiffness, cfg->density, s, &err)) return fail(PD_ERR_INVALID_ARGUMENT, "OBJ: " + err);
+  std::memcpy(pos, s.x.data(), s.x.size() * sizeof(double));
+  std::memcpy(mass, s.m.data(), s.m.size() * sizeof(double));
+  std::memcpy(pinned, s.pinned.data(), s.pinned.size());
+  for (size_t e = 0; e < s.edges.size(); ++e) {
+    edges[2 * e] = s.edges[e].a;
+    edges[2 * e + 1] = s.edges[e].b;
+    rest[e] = s.edges[e].rest;
+    k[e] = s.edges[e].k;
+  }
+  return PD_OK;
+}
+
 // ---------------------------------------------------------------------------------- sim
 static int sceneFromMesh(const pd_mesh& m, pdg::Scene& s) {
   if (m.n_vertices <= 0 || !m.positions || !m.masses || !m.pinned)

@@ -5,7 +5,10 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <cctype>
+#include <cstdlib>
 #include <numeric>
+#include <string>
 
 namespace pdg {
 
@@ -830,6 +833,123 @@ bool makeGrid(const GridSpec& g, Scene& s) {
     case 3: s.pinned[(ny - 1) * nx] = 1; break;
     default: break;
   }
+  s.v.assign(3 * static_cast<size_t>(n), 0.0);
+  s.q = s.x;
+  return true;
+}
+
+
+namespace {
+
+// Whitespace-separated tokens of one line.
+std::vector<std::string> tokensOf(const std::string& line) {
+  std::vector<std::string> out;
+  size_t i = 0;
+  while (i < line.size()) {
+    while (i < line.size() && std::isspace(static_cast<unsigned char>(line[i]))) ++i;
+    size_t j = i;
+    while (j < line.size() && !std::isspace(static_cast<unsigned char>(line[j]))) ++j;
+    if (j > i) out.emplace_back(line, i, j - i);
+    i = j;
+  }
+  return out;
+}
+
+}  // namespace
+
+bool makeObj(const std::string& text, double stiffness, double density, Scene& s, std::string* err) {
+  auto failWith = [&](const std::string& m) {
+    if (err) *err = m;
+    return false;
+  };
+  std::vector<double> pos;
+  std::vector<int> tri;
+  size_t start = 0;
+  int lineNo = 0;
+  while (start <= text.size()) {
+    size_t end = text.find('\n', start);
+    if (end == std::string::npos) end = text.size();
+    const std::string line = text.substr(start, end - start);
+    start = end + 1;
+    ++lineNo;
+    const std::vector<std::string> tok = tokensOf(line);
+    if (tok.empty()) continue;
+    if (tok[0] == "v") {
+      double c[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < 3 && k + 1 < static_cast<int>(tok.size()); ++k) {
+        char* e = nullptr;
+        c[k] = std::strtod(tok[k + 1].c_str(), &e);
+        if (e == tok[k + 1].c_str() || *e != '\0') return failWith("line " + std::to_string(lineNo) + ": bad coordinate");
+      }
+      pos.insert(pos.end(), c, c + 3);
+    } else if (tok[0] == "f") {
+      if (tok.size() < 4) continue;  // fewer than three corners: skipped, as the reference does
+      for (int k = 0; k < 3; ++k) {
+        const std::string first = tok[k + 1].substr(0, tok[k + 1].find('/'));
+        char* e = nullptr;
+        const long idx = std::strtol(first.c_str(), &e, 10);
+        if (e == first.c_str()) return failWith("line " + std::to_string(lineNo) + ": bad face index");
+        tri.push_back(static_cast<int>(idx) - 1);
+      }
+    }
+  }
+  const int n = static_cast<int>(pos.size() / 3);
+  if (n == 0 || tri.empty()) return failWith("no vertices or no triangles");
+  for (int i : tri)
+    if (i < 0 || i >= n) return failWith("face index out of range (indices are 1-based, negative ones unsupported)");
+  s = Scene{};
+  s.n = n;
+  s.x = pos;
+  // unique triangle edges in first-seen order, oriented as first seen
+  std::vector<uint64_t> seen;
+  seen.reserve(tri.size());
+  for (size_t t = 0; t < tri.size(); t += 3) {
+    for (int k = 0; k < 3; ++k) {
+      const int a = tri[t + k], b = tri[t + (k + 1) % 3];
+      if (a == b) continue;
+      const uint64_t key = (static_cast<uint64_t>(std::min(a, b)) << 32) | static_cast<uint32_t>(std::max(a, b));
+      seen.push_back(key);
+    }
+  }
+  {
+    std::vector<uint64_t> sorted = seen;
+    std::sort(sorted.begin(), sorted.end());
+    std::vector<uint8_t> used(sorted.size(), 0);
+    for (size_t t = 0; t < tri.size(); t += 3) {
+      for (int k = 0; k < 3; ++k) {
+        const int a = tri[t + k], b = tri[t + (k + 1) % 3];
+        if (a == b) continue;
+        const uint64_t key = (static_cast<uint64_t>(std::min(a, b)) << 32) | static_cast<uint32_t>(std::max(a, b));
+        const size_t at = static_cast<size_t>(std::lower_bound(sorted.begin(), sorted.end(), key) - sorted.begin());
+        // duplicates of a key are adjacent in `sorted`; the first occurrence claims them all
+        if (used[at]) continue;
+        for (size_t u = at; u < sorted.size() && sorted[u] == key; ++u) used[u] = 1;
+        const double dx = s.x[3 * b] - s.x[3 * a], dy = s.x[3 * b + 1] - s.x[3 * a + 1],
+                     dz = s.x[3 * b + 2] - s.x[3 * a + 2];
+        s.edges.push_back(Edge{a, b, std::sqrt(dx * dx + dy * dy + dz * dz), stiffness});
+      }
+    }
+  }
+  // surface masses: each triangle adds density·area/3 to its corners, in triangle order
+  const double rho = density > 0.0 ? density : 1.0;
+  s.m.assign(n, 0.0);
+  for (size_t t = 0; t < tri.size(); t += 3) {
+    const double* p0 = &s.x[3 * tri[t]];
+    const double* p1 = &s.x[3 * tri[t + 1]];
+    const double* p2 = &s.x[3 * tri[t + 2]];
+    const double u0 = p1[0] - p0[0], u1 = p1[1] - p0[1], u2 = p1[2] - p0[2];
+    const double w0 = p2[0] - p0[0], w1 = p2[1] - p0[1], w2 = p2[2] - p0[2];
+    const double c0 = u1 * w2 - u2 * w1, c1 = u2 * w0 - u0 * w2, c2 = u0 * w1 - u1 * w0;
+    const double area = 0.5 * std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    for (int k = 0; k < 3; ++k) s.m[tri[t + k]] += rho * area / 3.0;
+  }
+  double minPos = 1e300;
+  for (double m : s.m)
+    if (m > 1e-12) minPos = std::min(minPos, m);
+  if (minPos > 1e299) minPos = 1.0;
+  for (double& m : s.m)
+    if (m < 1e-12) m = minPos;
+  s.pinned.assign(n, 0);
   s.v.assign(3 * static_cast<size_t>(n), 0.0);
   s.q = s.x;
   return true;

@@ -124,6 +124,13 @@ struct GridSpec {
 bool gridCounts(const GridSpec& g, int* nv, int* ne, int* nb);
 bool makeGrid(const GridSpec& g, Scene& s);
 
+// Triangle mesh from OBJ text (Mesh::loadObj + makeScene's surface masses, core/mesh/Mesh.cpp:56-153,
+// core/sim/Scene.cpp:44-64): "v x y z" vertices, the first three corner indices of each "f" line
+// ("a", "a/b", "a/b/c", "a//c"; 1-based); distance constraints are the triangles' unique edges in
+// first-seen order at `stiffness`; masses density·area/3 per corner; no pins. False with a message
+// for a file the reference could not load or would index out of range.
+bool makeObj(const std::string& text, double stiffness, double density, Scene& s, std::string* err);
+
 // Hashes that decide refactorization (core/assemble/Assembler.cpp:29-92).
 struct Stamp {
   uint64_t k = 0, m = 0, pin = 0, dt = 0, structure = 0;

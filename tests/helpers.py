@@ -30,3 +30,30 @@ def max_rel(a, b):
     b = np.asarray(b, np.float64)
     scale = max(np.max(np.abs(b)), 1e-300)
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def obj_sheet(nx=9, ny=7, seed=0, curved=True):
+    """OBJ text of a triangulated nx×ny sheet (two triangles per quad, alternating diagonals),
+    vertices listed in a seeded random order and faces written in mixed token styles."""
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(nx * ny)          # file position of grid vertex g
+    inv = np.empty_like(order)
+    inv[order] = np.arange(nx * ny)
+    lines = ["# sheet", "o sheet"]
+    for p in range(nx * ny):
+        g = int(inv[p])
+        i, j = g % nx, g // nx
+        x, y = i / (nx - 1), j / (ny - 1)
+        z = 0.08 * np.sin(3.0 * x) * np.cos(2.0 * y) if curved else 0.0
+        lines.append(f"v {x:.9f} {z:.9f} {y:.9f}")
+    styles = ["{}", "{}/{}", "{}/{}/{}", "{}//{}"]
+    f = 0
+    for j in range(ny - 1):
+        for i in range(nx - 1):
+            a, b, c, d = j * nx + i, j * nx + i + 1, (j + 1) * nx + i + 1, (j + 1) * nx + i
+            tris = [(a, b, c), (a, c, d)] if (i + j) % 2 == 0 else [(a, b, d), (b, c, d)]
+            for t in tris:
+                st = styles[f % 4]
+                f += 1
+                lines.append("f " + " ".join(st.format(*([int(order[v]) + 1] * st.count("{}"))) for v in t))
+    return "\n".join(lines) + "\n"

@@ -125,3 +125,27 @@ def test_config_defaults_match_the_c_abi(pdg):
     with pytest.raises(pdg.PdError) as e:
         scene_factor(base, pdg.SceneConfig(cheb_mode=3))
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("seed,curved", [(0, True), (1, False), (2, True)])
+def test_obj_mesh_matches_oracle_bitwise(pdg, oracle, seed, curved):
+    """pd_make_obj against the oracle's restated Mesh::loadObj: vertices, unique edges in
+    first-seen order, rest lengths and surface masses bit for bit, then colouring and factor."""
+    from tests.helpers import obj_sheet
+    text = obj_sheet(11, 8, seed=seed, curved=curved)
+    cfg = pdg.SceneConfig(stiffness=777.0, density=1.7)
+    scene = pdg.make_obj(text, cfg)
+    om = oracle.make_obj(text, stiffness=777.0, density=1.7)
+    for a, b in [("positions", "positions"), ("masses", "masses"), ("edges", "edges"), ("edge_rest", "edge_rest"),
+                 ("edge_stiffness", "edge_k")]:
+        x, y = getattr(scene, a), getattr(om, b)
+        assert x.shape == y.shape and np.array_equal(bits(x) if x.dtype == np.float64 else x,
+                                                     bits(y) if y.dtype == np.float64 else y), a
+    assert not np.any(scene.pinned) and scene.bends.shape[0] == 0
+    scene.pinned[[0, 5]] = 1
+    f, info = scene_factor(scene, cfg)
+    orc = oracle_twin(scene, cfg, perm=f["perm"])
+    of = orc.factor()
+    assert np.array_equal(of["colptr"], f["colptr"]) and np.array_equal(bits(of["val"]), bits(f["val"]))
+    with pytest.raises(pdg.PdError):
+        pdg.make_obj("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 9\n", cfg)

@@ -359,3 +359,26 @@ def test_oracle_gradient_matches_central_differences():
     # the state is left unchanged and the loss-only call agrees
     assert np.array_equal(orc.state()[0], x0)
     assert orc.gradient(S, targets, force, grad=False)["loss"] == g["loss"]
+
+
+# ---------------------------------------------------------- OBJ meshes (core/mesh/Mesh.cpp:56-153)
+def test_obj_known_answers(oracle):
+    tri = "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n"
+    m = oracle.make_obj(tri, stiffness=500.0, density=3.0)
+    assert m.edges.tolist() == [[0, 1], [1, 2], [2, 0]]
+    assert np.allclose(m.edge_rest, [1.0, math.sqrt(2.0), 1.0], rtol=0, atol=1e-15)
+    assert np.all(m.edge_k == 500.0)
+    assert np.allclose(m.masses, 3.0 * 0.5 / 3.0, rtol=0, atol=1e-16)
+    # a quad as two triangles in slash styles; a four-index face keeps its first three corners
+    quad = "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1/1 2/2 3/3\nf 1//1 3//3 4//4 2//2\n"
+    m = oracle.make_obj(quad, density=1.0)
+    assert m.edges.tolist() == [[0, 1], [1, 2], [2, 0], [2, 3], [3, 0]]
+    assert np.allclose(m.masses, [1 / 3, 1 / 6, 1 / 3, 1 / 6], rtol=0, atol=1e-16)
+    # a repeated corner adds no edge; an unused vertex takes the smallest positive mass
+    deg = "v 0 0 0\nv 2 0 0\nv 0 2 0\nv 5 5 5\nf 1 2 3\nf 1 1 2\n"
+    m = oracle.make_obj(deg)
+    assert len(m.edges) == 3 and m.masses[3] == m.masses[0]
+    for bad in ("v 0 0 0\n", "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 x\n", "v 0 0 0\nv 1 0 0\nf 1 2 3\n",
+                "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 0 1 2\n"):
+        with pytest.raises(ValueError):
+            oracle.make_obj(bad)
