@@ -237,7 +237,9 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oXhl = I.oXhatHl = 0;
   I.teamECap = I.teamBCap = I.teamWCap = 0;
   if (denseKind == 1 || denseKind == 2) {
-    I.oAinv = A.add(pdg::denseInverse32(I.F, &I.denseLd));
+    // Ã⁻¹ (FP32, rows padded to 32) is filled on the GPU after the upload (launchDenseInverse)
+    I.denseLd = static_cast<int>((n + 31) / 32 * 32);
+    I.oAinv = A.zeros(4 * n * static_cast<size_t>(I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
     I.oVcol = A.add(I.L.col);
     I.oVval = A.add(I.L.val);
@@ -719,7 +721,15 @@ struct pd_sim {
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
     PD_CUDA(cudaMemcpy(dArena, A.host.data(), A.host.size(), cudaMemcpyHostToDevice));
-    return ensureLogs(capacity);
+    const int rc = ensureLogs(capacity);
+    if (rc != PD_OK) return rc;
+    for (size_t i = 0; i < inst.size(); ++i) {  // explicit inverses from the uploaded FP64 factors
+      if (inst[i].denseLd <= 0) continue;
+      const int e = pdg::launchDenseInverse(dDesc + i, inst[i].scene.n, stream);
+      if (e != 0) return cudaFail(static_cast<cudaError_t>(e), "explicit inverse launch");
+    }
+    PD_CUDA(cudaStreamSynchronize(stream));  // complete before a later stream change can race it
+    return PD_OK;
   }
 
   int ensureLogs(int capacity) {

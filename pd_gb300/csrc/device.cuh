@@ -194,6 +194,9 @@ struct GradDev {
 int launchGradient(const InstanceDev* dInstances, const GradDev* dGrads, int count, int clusterSize, int substeps,
                    int smemBytes, void* stream);
 int gradClusterSupported(int clusterSize);
+// Fills the instance's Ã⁻¹ (FP32, rows denseLd apart) from its FP64 supernodal factor: three
+// columns per CTA, one in each component of the solve.
+int launchDenseInverse(const InstanceDev* dInstance, int n, void* stream);
 
 constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per

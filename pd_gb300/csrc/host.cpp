@@ -466,32 +466,6 @@ void buildMixed(Factor& f, const ScalarMatrix& A) {
   }
 }
 
-std::vector<float> denseInverse32(const Factor& f, int* ldOut) {
-  const int n = f.n;
-  const int ld = (n + 31) / 32 * 32;
-  *ldOut = ld;
-  std::vector<float> M(static_cast<size_t>(n) * ld, 0.0f);
-  std::vector<double> w(n);
-  for (int v = 0; v < n; ++v) {  // column v of Ã⁻¹ = solve(e_v)
-    std::fill(w.begin(), w.end(), 0.0);
-    w[f.iperm[v]] = 1.0;
-    for (int k = 0; k < n; ++k) {
-      const double yk = w[k];
-      if (yk != 0.0)
-        for (int p = f.colptr[k]; p < f.colptr[k + 1]; ++p) w[f.rowidx[p]] -= f.colval[p] * yk;
-    }
-    for (int k = 0; k < n; ++k) w[k] *= f.dinv[k];
-    for (int k = n - 1; k >= 0; --k) {
-      double acc = w[k];
-      for (int p = f.colptr[k]; p < f.colptr[k + 1]; ++p) acc -= f.colval[p] * w[f.rowidx[p]];
-      w[k] = acc;
-    }
-    float* row = M.data() + static_cast<size_t>(v) * ld;  // symmetric: row v = column v
-    for (int u = 0; u < n; ++u) row[u] = static_cast<float>(w[f.iperm[u]]);
-  }
-  return M;
-}
-
 std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
   const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
   std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);

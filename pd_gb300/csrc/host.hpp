@@ -103,9 +103,7 @@ std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas);
 std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas = 1);
 // Fills the mixed-precision fields of a factorized Factor (needs the supernodal fields).
 void buildMixed(Factor& f, const ScalarMatrix& A);
-// Explicit inverse Ã⁻¹ in vertex order, FP32, rows padded to `ld` (a multiple of 32) entries:
-// computed column by column with the FP64 factor (Ã is symmetric, so columns are rows).
-std::vector<float> denseInverse32(const Factor& f, int* ld);
+
 // Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
 bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
 void buildSchedules(Factor& f);

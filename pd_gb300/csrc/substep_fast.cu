@@ -65,6 +65,28 @@ __global__ void __launch_bounds__(kBlockThreads) solveFastKernel(const InstanceD
   }
 }
 
+// Rows 3b, 3b+1, 3b+2 of Ã⁻¹ for b = blockIdx.x: the FP64 supernodal solve of three unit vectors
+// at once (column 3b + c in component c). Ã is symmetric, so a solved column is the row stored.
+__global__ void __launch_bounds__(kBlockThreads) denseInverseKernel(const InstanceDev* __restrict__ inst) {
+  extern __shared__ double smem[];
+  const InstanceDev& I = *inst;
+  const int n = I.n, v0 = 3 * static_cast<int>(blockIdx.x);
+  double* w = smem;
+  double* t = smem + 3 * n;
+  for (int i = threadIdx.x; i < 3 * n; i += blockDim.x) w[i] = 0.0;
+  __syncthreads();
+  if (threadIdx.x < 3 && v0 + static_cast<int>(threadIdx.x) < n)
+    w[3 * I.iperm[v0 + threadIdx.x] + threadIdx.x] = 1.0;
+  __syncthreads();
+  const Team<false> tm{0, 1};
+  TeamSolve<false>::run(I, tm, w, t);
+  float* A = const_cast<float*>(I.Ainv);
+  for (int c = 0; c < 3 && v0 + c < n; ++c) {
+    float* row = A + static_cast<size_t>(v0 + c) * I.denseLd;
+    for (int u = threadIdx.x; u < n; u += blockDim.x) row[u] = static_cast<float>(w[3 * I.iperm[u] + c]);
+  }
+}
+
 cudaLaunchConfig_t clusterConfig(int blocks, int clusterSize, int smemBytes, void* stream, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
@@ -114,6 +136,19 @@ int launchSubstepCluster(const InstanceDev* d, int count, int clusterSize, int s
   cudaLaunchConfig_t cfg = clusterConfig(count * clusterSize, clusterSize, 0, stream, attr);
   const cudaError_t e = cudaLaunchKernelEx(&cfg, substepClusterKernel, d, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
+}
+
+int launchDenseInverse(const InstanceDev* d, int n, void* stream) {
+  if (n <= 0) return 0;
+  const int smem = 48 * n;
+  if (smem > 200 * 1024) return static_cast<int>(cudaErrorInvalidValue);
+  static bool attrSet = false;
+  if (!attrSet) {
+    cudaFuncSetAttribute(denseInverseKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attrSet = true;
+  }
+  denseInverseKernel<<<(n + 2) / 3, kBlockThreads, smem, static_cast<cudaStream_t>(stream)>>>(d);
+  return static_cast<int>(cudaGetLastError());
 }
 
 int launchSolveFast(const InstanceDev* d, const double* b, double* x, int smemBytes, void* stream) {
