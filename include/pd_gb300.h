@@ -239,6 +239,16 @@ int pd_sim_set_pinned(pd_sim* s, int32_t instance, const uint8_t* pinned, const 
 int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg);
 int pd_sim_get_info(pd_sim* s, int32_t instance, pd_sim_info* out);
 int pd_sim_get_stats(pd_sim* s, int32_t instance, pd_sim_stats* out);
+/* Per-iteration residual trace, for convergence studies like the reference's
+ * _verify/residual_trace.cpp (r_k within one substep): while enabled, every launch records for each
+ * substep and iteration k = 1..max_iterations the residual the gate saw after iteration k
+ * (Integrator.cpp:230-263: max over free vertices of |unbalanced force| / m), NaN where the substep
+ * stopped earlier. Recorded only with the residual gate (residual_tolerance > 0; a tiny tolerance
+ * traces without early exits). out: substeps × max_iterations doubles of instance i from the last
+ * pd_sim_step, substeps ≤ that call's count. */
+int pd_sim_set_residual_trace(pd_sim* s, int32_t enable);
+int pd_sim_get_residual_trace(pd_sim* s, int32_t i, double* out, int32_t substeps);
+
 /* Per-substep iteration counts / gate flags of the last pd_sim_step (count = its substeps). */
 int pd_sim_iteration_log(pd_sim* s, int32_t instance, int32_t* iterations, uint8_t* converged, int32_t count);
 /* Exports the factor (perm[n], colptr[n+1], rowidx[nnz], val[nnz], dinv[n]; NULL parts skipped);

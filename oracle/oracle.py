@@ -76,6 +76,8 @@ def lib():
     L.oracle_grid_counts.argtypes = [_P(_GridSpec), _P(C.c_int), _P(C.c_int), _P(C.c_int)]
     L.oracle_make_grid.argtypes = [_P(_GridSpec), dp, dp, u8p, ip, dp, dp, ip, dp]
     L.oracle_make_grid.restype = C.c_int
+    L.oracle_sim_step_traced.argtypes = [C.c_void_p, C.c_int, dp]
+    L.oracle_sim_step_traced.restype = C.c_int
     L.oracle_obj_counts.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int)]
     L.oracle_obj_counts.restype = C.c_int
     L.oracle_make_obj.argtypes = [C.c_char_p, C.c_double, C.c_double, dp, dp, u8p, ip, dp, dp]
@@ -272,6 +274,15 @@ class OracleSim:
         if rc != 0:
             raise RuntimeError("oracle factorization failed")
         return it, cv
+
+    def step_traced(self, substeps):
+        """Steps, returning the gate residual after every iteration: (substeps, K) with NaN past
+        each substep's last iteration."""
+        K = max(1, self.cfg.max_iterations)
+        out = np.zeros((substeps, K))
+        if self._L.oracle_sim_step_traced(self._h, substeps, _ptr(out, C.c_double)) != 0:
+            raise RuntimeError("oracle step failed")
+        return out
 
     def state(self):
         x = np.zeros((self.n, 3))

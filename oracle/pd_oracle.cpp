@@ -100,6 +100,7 @@ struct oracle_sim {
   int factorizeCount = 0, analyzeCount = 0, iterationsUsed = 0, earlyExitCount = 0;
   bool converged = false;
   double lastResidual = -1.0;
+  std::vector<double>* trace = nullptr;  // when set: the gate residual of every iteration, appended
 };
 
 namespace {
@@ -798,6 +799,7 @@ int stepOnce(oracle_sim& s) {
           resHit = (residual <= cfg.residual_tolerance * gScale);
         }
         s.lastResidual = residual;
+        if (s.trace) s.trace->push_back(residual);
         const bool conv = (cfg.residual_tolerance > 0.0) ? resHit : (absHit || relHit);
         s.converged = conv;
         if (conv) s.earlyExitCount += 1;
@@ -1119,6 +1121,20 @@ extern "C" int oracle_sim_step(oracle_sim* s, int substeps, int32_t* iters, uint
     if (conv) conv[k] = s->converged ? 1 : 0;
   }
   return 0;
+}
+
+extern "C" int oracle_sim_step_traced(oracle_sim* s, int substeps, double* trace) {
+  const int K = std::max(1, s->cfg.max_iterations);
+  std::vector<double> t;
+  s->trace = &t;
+  int rc = 0;
+  for (int k = 0; k < substeps && rc == 0; ++k) {
+    t.clear();
+    if (stepOnce(*s) < 0) rc = -1;
+    for (int j = 0; j < K; ++j) trace[static_cast<size_t>(k) * K + j] = j < static_cast<int>(t.size()) ? t[j] : NAN;
+  }
+  s->trace = nullptr;
+  return rc;
 }
 
 extern "C" void oracle_sim_get_state(const oracle_sim* s, double* pos, double* vel) {

@@ -95,6 +95,9 @@ void oracle_sim_destroy(oracle_sim* s);
 
 /* Runs `substeps` calls of stepOnce. iterations / converged (nullable) receive per-substep values. */
 int oracle_sim_step(oracle_sim* s, int substeps, int32_t* iterations, uint8_t* converged);
+/* The same, recording the gate residual after every iteration: trace[k·K + j] for substep k and
+ * iteration j + 1 (K = max(1, max_iterations); NaN past the substep's last iteration). */
+int oracle_sim_step_traced(oracle_sim* s, int substeps, double* trace);
 
 void oracle_sim_get_state(const oracle_sim* s, double* positions, double* velocities);
 void oracle_sim_set_state(oracle_sim* s, const double* positions, const double* velocities);

@@ -130,6 +130,8 @@ _SIGS = {
     "pd_sim_set_config": ([C.c_void_p, C.POINTER(_Cfg)], C.c_int),
     "pd_sim_get_info": ([C.c_void_p, C.c_int32, C.POINTER(_SimInfo)], C.c_int),
     "pd_sim_get_stats": ([C.c_void_p, C.c_int32, C.POINTER(_SimStats)], C.c_int),
+    "pd_sim_set_residual_trace": ([C.c_void_p, C.c_int32], C.c_int),
+    "pd_sim_get_residual_trace": ([C.c_void_p, C.c_int32, _dp, C.c_int32], C.c_int),
     "pd_sim_iteration_log": ([C.c_void_p, C.c_int32, _ip, _u8p, C.c_int32], C.c_int),
     "pd_sim_get_factor": ([C.c_void_p, C.c_int32, _ip, _ip, _ip, _dp, _dp, C.POINTER(C.c_int64)], C.c_int),
     "pd_sim_solve": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
@@ -353,6 +355,7 @@ class Simulator:
         self._h = h
         self.count = len(scenes)
         self._last = 0
+        self._cfgs = list(cfgs)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -418,6 +421,7 @@ class Simulator:
     def set_config(self, cfg: SceneConfig):
         c = cfg.c()
         _check(self._lib.pd_sim_set_config(self._h, C.byref(c)))
+        self._cfgs = [cfg] * self.count
 
     def info(self, i: int = 0) -> dict:
         s = _SimInfo()
@@ -468,6 +472,17 @@ class Simulator:
         cv = np.zeros(self._last, np.uint8)
         _check(self._lib.pd_sim_iteration_log(self._h, i, _ptr(it, C.c_int32), _ptr(cv, C.c_uint8), self._last))
         return it, cv
+
+    def set_residual_trace(self, enable: bool = True):
+        """Record the gate residual after every iteration of every substep (pd_sim_set_residual_trace)."""
+        _check(self._lib.pd_sim_set_residual_trace(self._h, 1 if enable else 0))
+
+    def residual_trace(self, i: int = 0):
+        """(substeps of the last step, max_iterations) residuals, NaN past each substep's last iteration."""
+        k = max(1, self._cfgs[i].max_iterations)
+        out = np.zeros((self._last, k))
+        _check(self._lib.pd_sim_get_residual_trace(self._h, i, _ptr(out, C.c_double), self._last))
+        return out
 
     def factor(self, i: int = 0) -> dict:
         nnz = C.c_int64()

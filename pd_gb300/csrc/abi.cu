@@ -411,7 +411,7 @@ std::vector<double> chebWeights(const pd_scene_config& c) {
 }
 
 pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog,
-                          const double* omega) {
+                          const double* omega, double* resTrace) {
   auto P = [&](size_t off) { return base + off; };
   const auto& c = I.cfg;
   const auto& s = I.scene;
@@ -441,6 +441,7 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.xsol = reinterpret_cast<double*>(P(I.oXsol));
   d.chebFrom = chebFrom(c);
   d.omega = omega;
+  d.resTrace = resTrace;
   d.bbase = reinterpret_cast<double*>(P(I.oBbase));
   d.m = reinterpret_cast<const double*>(P(I.oM));
   d.pinned = reinterpret_cast<const uint8_t*>(P(I.oPin));
@@ -558,6 +559,10 @@ struct pd_sim {
   pdg::InstanceDev* dDescOrder = nullptr;  // batch descriptors by decreasing cost (correction kernel)
   double* dOmega = nullptr;                // over-relaxation weights of every instance
   size_t omegaCap = 0;
+  bool traceOn = false;                    // record each iteration's gate residual
+  double* dTrace = nullptr;                // per instance logCapacity × max_iterations
+  size_t traceCap = 0, traceLen = 0;
+  std::vector<size_t> traceOff;
   int32_t* dIterLog = nullptr;
   uint8_t* dConvLog = nullptr;
   int logCapacity = 0;
@@ -701,6 +706,9 @@ struct pd_sim {
     if (dDesc) cudaFree(dDesc);
     if (dDescOrder) cudaFree(dDescOrder);
     if (dOmega) cudaFree(dOmega);
+    if (dTrace) cudaFree(dTrace);
+    dTrace = nullptr;
+    traceCap = traceLen = 0;
     if (dIterLog) cudaFree(dIterLog);
     if (dConvLog) cudaFree(dConvLog);
     dArena = nullptr;
@@ -767,9 +775,21 @@ struct pd_sim {
     }
     if (!weights.empty())
       PD_CUDA(cudaMemcpy(dOmega, weights.data(), sizeof(double) * weights.size(), cudaMemcpyHostToDevice));
+    // residual trace: logCapacity × max_iterations per instance
+    traceOff.assign(inst.size() + 1, 0);
+    for (size_t i = 0; i < inst.size(); ++i)
+      traceOff[i + 1] = traceOff[i] + static_cast<size_t>(logCapacity) * std::max(1, inst[i].cfg.max_iterations);
+    traceLen = traceOn ? traceOff.back() : 0;
+    if (traceLen > traceCap) {
+      if (dTrace) cudaFree(dTrace);
+      dTrace = nullptr;
+      traceCap = 0;
+      PD_CUDA(cudaMalloc(&dTrace, sizeof(double) * traceLen));
+      traceCap = traceLen;
+    }
     for (size_t i = 0; i < inst.size(); ++i) {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity,
-                              dOmega ? dOmega + wOff[i] : nullptr));
+                              dOmega ? dOmega + wOff[i] : nullptr, traceOn ? dTrace + traceOff[i] : nullptr));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
       int rows = 0;
       const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
@@ -1129,6 +1149,7 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
     if (rc != PD_OK) return rc;
   }
   const int count = static_cast<int>(s->inst.size());
+  if (s->traceOn && s->traceLen) PD_CUDA(cudaMemsetAsync(s->dTrace, 0xFF, sizeof(double) * s->traceLen, s->stream));
   int rc;
   const int p = s->precision();
   if (p == PD_PRECISION_FP64_EXACT) {
@@ -1352,6 +1373,26 @@ int pd_sim_iteration_log(pd_sim* s, int32_t i, int32_t* iters, uint8_t* conv, in
   if (const int rc_ = s->sync()) return rc_;
   if (iters) PD_CUDA(cudaMemcpy(iters, s->dIterLog + static_cast<size_t>(i) * s->logCapacity, 4 * count, cudaMemcpyDeviceToHost));
   if (conv) PD_CUDA(cudaMemcpy(conv, s->dConvLog + static_cast<size_t>(i) * s->logCapacity, count, cudaMemcpyDeviceToHost));
+  return PD_OK;
+}
+
+int pd_sim_set_residual_trace(pd_sim* s, int32_t enable) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (const int rc_ = s->sync()) return rc_;
+  s->traceOn = enable != 0;
+  return s->writeDescriptors();
+}
+
+int pd_sim_get_residual_trace(pd_sim* s, int32_t i, double* out, int32_t substeps) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
+  if (!s->traceOn) return fail(PD_ERR_STATE, "the residual trace is not enabled");
+  if (substeps < 0 || substeps > s->lastSubsteps)
+    return fail(PD_ERR_INVALID_ARGUMENT, "substeps exceeds the last step's substeps");
+  if (const int rc_ = s->sync()) return rc_;
+  const size_t k = static_cast<size_t>(std::max(1, s->inst[i].cfg.max_iterations));
+  PD_CUDA(cudaMemcpy(out, s->dTrace + s->traceOff[i], sizeof(double) * k * substeps, cudaMemcpyDeviceToHost));
   return PD_OK;
 }
 

@@ -118,6 +118,8 @@ struct InstanceDev {
   const int32_t* window;       // 2 × team: vertex range [lo, hi) whose positions a CTA reads
   int32_t* err;                // set when an exchange gave up waiting
   // statistics
+  double* resTrace;      // null, or per substep of the current launch maxIter values: the gate's
+                         // residual after each iteration (NaN for iterations not run)
   int32_t* iterLog;      // per substep of the current launch
   uint8_t* convLog;
   double* lastResidual;  // scalar

@@ -270,6 +270,7 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
       __syncthreads();
       used = k + 1;
       lastRes = I.useResidual ? res : -1.0;
+      if (I.resTrace && I.useResidual && threadIdx.x == 0) I.resTrace[(size_t)step * I.maxIter + k] = res;
       conv = *flag != 0;
       __syncthreads();
       if (conv) break;

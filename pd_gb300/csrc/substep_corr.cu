@@ -255,6 +255,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       if (I.useResidual && k >= 1 && k - 1 < I.chebFrom) {
         lastRes = resMax;
         used = k;
+        if (I.resTrace && TID == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = resMax;
         conv = resMax <= I.resThreshold;
         stop = stop || conv;
       }
@@ -301,6 +302,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
         tm.sync();
         lastRes = resSolve;
         used = k + 1;
+        if (I.resTrace && TID == 0) I.resTrace[(size_t)step * I.maxIter + k] = resSolve;
         conv = resSolve <= I.resThreshold;
         if (conv || k + 1 == I.maxIter) break;
         continue;

@@ -356,6 +356,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (I.useResidual && k >= 1) {
         lastRes = gateA;
         used = k;
+        if (I.resTrace && rank == 0 && threadIdx.x == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gateA;
         conv = gateA <= I.resThreshold;
         stop = stop || conv;
       }

@@ -196,6 +196,7 @@ __device__ void runSubstepsMixed(const InstanceDev& I, const Team<CLUSTER>& tm, 
       conv = I.useResidual ? (res <= I.resThreshold) : (absHit || relHit);
       used = k + 1;
       lastRes = I.useResidual ? res : -1.0;
+      if (I.resTrace && I.useResidual && T == 0) I.resTrace[(size_t)step * I.maxIter + k] = res;
       if (conv) break;
     }
     for (int v = T; v < I.n; v += NT) {  // velocity, damping, pin resnap (Integrator.cpp:774-791)
@@ -386,6 +387,7 @@ __device__ void runSubstepsDense(const InstanceDev& I, const Team<true>& tm, int
       conv = I.useResidual ? (res <= I.resThreshold) : (absHit || relHit);
       used = k + 1;
       lastRes = I.useResidual ? res : -1.0;
+      if (I.resTrace && I.useResidual && T == 0) I.resTrace[(size_t)step * I.maxIter + k] = res;
       if (conv) break;
     }
     for (int v = T; v < n; v += NT) {  // velocity, damping, pin resnap (Integrator.cpp:774-791)

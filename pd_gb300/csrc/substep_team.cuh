@@ -399,6 +399,7 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
       conv = I.useResidual ? (res <= I.resThreshold) : (absHit || relHit);
       used = k + 1;
       lastRes = I.useResidual ? res : -1.0;
+      if (I.resTrace && I.useResidual && T == 0) I.resTrace[(size_t)step * I.maxIter + k] = res;
       if (conv) break;
     }
     for (int v = T; v < I.n; v += NT) {  // velocity, damping, pin resnap

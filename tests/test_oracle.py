@@ -382,3 +382,16 @@ def test_obj_known_answers(oracle):
                 "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 0 1 2\n"):
         with pytest.raises(ValueError):
             oracle.make_obj(bad)
+
+
+def test_residual_trace_matches_gate(oracle):
+    """step_traced records every iteration's gate residual: as many as the iterations used, the
+    last one the stats' last residual, NaN after an early exit."""
+    m = oracle.make_grid(oracle.GridSpec(nx=12, ny=12, spacing=0.05, stiffness=K))
+    cfg = oracle.Config(dt=H, max_iterations=30, residual_tolerance=0.6)
+    a, b = oracle.OracleSim(m, cfg), oracle.OracleSim(m, cfg)
+    tr = a.step_traced(20)
+    it, _ = b.step(20)
+    assert np.array_equal((~np.isnan(tr)).sum(axis=1), it) and (it < 30).any()
+    last = tr[-1][~np.isnan(tr[-1])][-1]
+    assert last == a.stats()["last_residual"] == b.stats()["last_residual"]
