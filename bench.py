@@ -38,6 +38,8 @@ PRECISIONS = {"fp64-exact": (0, "f64"), "fp64": (1, "f64"), "fp32-projection": (
               "fp32-solve": (3, "f64 (f32 solve + f64 refinement)"),
               "mixed": (4, "f32 (positions as f32 hi/lo pairs)")}
 POS_ERR_BOUND = 1e-5
+# σ of the finite-difference directions in scaled units (relative κ, m/s, vertex weights)
+FD_SCALE = 100.0
 
 
 def kernel_name(info):
@@ -425,21 +427,19 @@ def run_ours(args):
     count = len(scenes)
     value = world * count * args.steps / t_max  # aggregate (cloth-)substeps/s
 
-    # ---- e2e: through the C ABI, every cloth's state copied from pinned host memory and read
-    # back every step
+    # ---- e2e: through the C ABI's host-state call (pd_sim_step_host): every step copies every
+    # cloth's positions and velocities in from pinned host memory, runs the substep and copies
+    # them back (gather kernel → substep → scatter kernel, one CUDA graph replay), and returns
+    # when the results are in host memory
     host = []
     for i in range(count):
         x0, v0 = sim.state(i)
         host.append((torch.from_numpy(x0.copy()).pin_memory(), torch.from_numpy(v0.copy()).pin_memory()))
-    hosts = [(hx.numpy(), hv.numpy()) for hx, hv in host]
     sim.set_stream(None)
+    sim.bind_host([hx.numpy() for hx, _ in host], [hv.numpy() for _, hv in host])
 
     def e2e_step():
-        for i, (hx, hv) in enumerate(hosts):
-            sim.set_state(i, hx, hv)           # H2D from pinned memory: positions + velocities
-        sim.step(1, sync=False)
-        for i, (hx, hv) in enumerate(hosts):
-            sim.state(i, out_x=hx, out_v=hv)   # D2H into pinned memory (the first waits for the step)
+        sim.step_host(1)
 
     for _ in range(args.warmup):
         e2e_step()
@@ -486,7 +486,9 @@ def run_ours(args):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": kernel, "algorithmic_bytes_per_launch": per_launch_bytes},
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "call": "pd_sim_step_host (gather kernel, substep, scatter kernel: one CUDA graph)"
+                        if info["host_state"] == P.PD_HOST_STATE_GRAPH else "pd_sim_step_host (cudaMemcpyAsync per array)"},
                 "clocks": clocks}
         if PRECISIONS[args.precision][0] <= 1:
             ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
@@ -589,14 +591,20 @@ def run_gradients(args):
     dt = time.perf_counter() - t0
     clocks = sampler.stop()
     value = count * args.steps / dt
-    # central differences of the loss of problem 0 along random directions, one batched launch each
+    # central differences of the loss of problem 0 along random directions, one batched launch each.
+    # The FP64 loss carries ~2e-10 relative rounding noise (the forward map over 1200 solves), so a
+    # difference quotient resolves 1e-6 only when the step moves the loss by ~1e-4 of itself: the
+    # directions are drawn in scaled units — each κ_e relative to itself, v₀ in m/s, the force in
+    # units of the vertex's weight — with σ = FD_SCALE, so that ε = 1e-6 moves every parameter by
+    # ~1e-4 of its scale (well inside the range where the O(ε²) truncation term is negligible)
     rng = np.random.default_rng(1)
     k0 = np.asarray(scene.edge_stiffness, np.float64)
+    weight = np.asarray(scene.masses, np.float64)[:, None] * 9.81
     g0 = grads[0]
-    dirs = [(k0 * rng.normal(0.0, 0.05, k0.shape), rng.normal(0.0, 0.1, (scene.n, 3)), rng.normal(0.0, 0.05, (scene.n, 3)))
-            for _ in range(args.fd_directions)]
+    dirs = [(k0 * rng.normal(0.0, FD_SCALE, k0.shape), rng.normal(0.0, FD_SCALE, (scene.n, 3)),
+             weight * rng.normal(0.0, FD_SCALE, (scene.n, 3))) for _ in range(args.fd_directions)]
     fd_err = {}
-    for eps in (1e-6, 1e-4):
+    for eps in (1e-6, 1e-5):
         fd_sim = P.Simulator([scene] * (2 * len(dirs)), [cfg] * (2 * len(dirs)))
         forces = []
         for j, (dk, dv, df) in enumerate(dirs):
@@ -606,7 +614,7 @@ def run_gradients(args):
                 fd_sim.set_state(i, scene.positions, sign * eps * dv)
                 forces.append(sign * eps * df)
         losses = fd_sim.gradient(S, [targets[0]] * (2 * len(dirs)), forces, grad=False)
-        errs, errs_n = [], []
+        errs, errs_n, fds, adjs = [], [], [], []
         for j, (dk, dv, df) in enumerate(dirs):
             fd = (losses[2 * j]["loss"] - losses[2 * j + 1]["loss"]) / (2 * eps)
             adj = g0["dkappa"] @ dk + np.sum(g0["dv0"] * dv) + np.sum(g0["dforce"] * df)
@@ -615,7 +623,11 @@ def run_gradients(args):
                      + np.linalg.norm(g0["dforce"]) * np.linalg.norm(df))
             errs.append(abs(fd - adj) / max(abs(adj), 1e-300))
             errs_n.append(abs(fd - adj) / max(scale, 1e-300))
+            fds.append(fd)
+            adjs.append(adj)
+        fds, adjs = np.array(fds), np.array(adjs)
         fd_err[f"eps_{eps:g}"] = {"max_rel": float(max(errs)), "median_rel": float(np.median(errs)),
+                                  "normwise_rel": float(np.linalg.norm(fds - adjs) / max(np.linalg.norm(adjs), 1e-300)),
                                   "max_rel_to_gradient_scale": float(max(errs_n))}
         del fd_sim
     # FP64 CPU reference gradient of problem 0
@@ -652,7 +664,8 @@ def run_gradients(args):
                          "kernel": "gradientClusterKernel" if info["cluster_ctas"] > 1 else "gradientKernel",
                          "algorithmic_bytes_per_launch": per_launch},
             "fp64": {"achieved_gops": fp64_gops, "peak_gops": 503.4, "frac": fp64_gops / 503.4},
-            "grad_check": {"fd_directions": len(dirs), **fd_err, "vs_cpu_reference_rel": rel,
+            "grad_check": {"fd_directions": len(dirs), "fd_direction_sigma": FD_SCALE,
+                           "fd_direction_units": "κ_e relative, v₀ m/s, force in vertex weights", **fd_err, "vs_cpu_reference_rel": rel,
                            "loss_problem0": g0["loss"], "loss_cpu_reference": r["loss"]},
             "clocks": clocks,
             "cpu_baseline": ({"value": 1.0 / cpu_s, "unit": "grads/s", "cores": 1, "kind": "port",

@@ -192,7 +192,12 @@ typedef struct pd_sim_info {
   int64_t device_bytes;          /* device memory held by this instance */
   int32_t cluster_ctas;          /* CTAs running each cloth */
   int32_t solve_kind;            /* PD_SOLVE_* */
+  int32_t host_state;            /* PD_HOST_STATE_*: how pd_sim_step_host moves the bound arrays */
 } pd_sim_info;
+
+#define PD_HOST_STATE_NONE 0     /* no host arrays bound */
+#define PD_HOST_STATE_COPIES 1   /* one cudaMemcpyAsync per array each way (pageable memory) */
+#define PD_HOST_STATE_GRAPH 2    /* gather / scatter kernels over the host link, one CUDA graph per call */
 
 /* How the substep kernel solves L·x = b. */
 #define PD_SOLVE_LEVELS 0        /* FP64 level-scheduled rows in the reference's order */
@@ -229,6 +234,23 @@ int pd_sim_get_state(pd_sim* s, int32_t instance, double* positions, double* vel
 int pd_sim_set_state(pd_sim* s, int32_t instance, const double* positions, const double* velocities);
 /* Device addresses of an instance's position / velocity arrays (3n doubles each). */
 int pd_sim_device_state(pd_sim* s, int32_t instance, double** positions, double** velocities);
+/* Host-state stepping: the reference's stepOnce on SimContext::mesh.positions / velocities, which
+ * live in host memory (core/sim/Integrator.cpp:312-797, core/sim/Scene.h:154-178), for a whole batch.
+ * pd_sim_bind_host registers one positions and one velocities array (3n doubles, [x,y,z] per
+ * vertex) per instance; they must stay allocated while bound (NULL, NULL unbinds). Each
+ * pd_sim_step_host call copies every bound array in, runs `substeps` substeps (0: the copies
+ * only) and copies them back, and returns when the results are in host memory.
+ * - Arrays that all lie in page-locked memory (cudaHostAlloc, cudaMallocHost, cudaHostRegister)
+ *   are read and written by one gather and one scatter kernel for the whole batch over the host
+ *   link, and gather → substeps → scatter is captured once as a CUDA graph and replayed on every
+ *   later call with the same substep count (recaptured after a refactorization, a pin-mask, dt or
+ *   trace change, or a new binding). pd_sim_get_info reports PD_HOST_STATE_GRAPH.
+ * - Otherwise each array is copied with its own cudaMemcpyAsync (PD_HOST_STATE_COPIES).
+ * - A non-finite position fails the call with PD_ERR_INVALID_ARGUMENT: before any work for
+ *   pageable arrays, after the step (whose results are then undefined) for page-locked ones.
+ * The handle's stream orders the work; on the default stream a private stream carries the graph. */
+int pd_sim_bind_host(pd_sim* s, double* const* positions, double* const* velocities);
+int pd_sim_step_host(pd_sim* s, int32_t substeps);
 /* Moves pin targets; only the RHS changes, no refactorization (core/assemble/Assembler.h:52-60). */
 int pd_sim_set_pin_positions(pd_sim* s, int32_t instance, const double* pin_positions);
 /* Changes edge stiffnesses; refactorizes (the stamp changes, Assembler.cpp:111-147). */

@@ -16,6 +16,9 @@ from .api import (  # noqa: F401
     PD_SOLVE_DENSE32,
     PD_SOLVE_DENSE32_TEAM,
     PD_SOLVE_SUPERNODAL32_CORRECTION,
+    PD_HOST_STATE_NONE,
+    PD_HOST_STATE_COPIES,
+    PD_HOST_STATE_GRAPH,
     PD_CHEB_OFF,
     PD_CHEB_RHO,
     PD_CHEB_INTERVAL,

@@ -27,6 +27,9 @@ PD_SOLVE_SUPERNODAL32 = 2
 PD_SOLVE_DENSE32 = 3
 PD_SOLVE_DENSE32_TEAM = 4
 PD_SOLVE_SUPERNODAL32_CORRECTION = 5
+PD_HOST_STATE_NONE = 0            # Simulator.info()["host_state"]: no host arrays bound
+PD_HOST_STATE_COPIES = 1          # step_host copies each pageable array with its own copy
+PD_HOST_STATE_GRAPH = 2           # step_host: gather/scatter kernels in one CUDA graph
 PD_CHEB_OFF = 0                   # SceneConfig.cheb_mode: plain PD iterations
 PD_CHEB_RHO = 1                   # ω recurrence from ρ after cheb_start plain iterations (PD_CHEB=1)
 PD_CHEB_INTERVAL = 2              # Chebyshev roots over [m − δ, m + δ] (PD_CHEB_MODE=interval)
@@ -76,7 +79,7 @@ class _SimInfo(C.Structure):
         ("color_count", C.c_int32), ("matrix_nnz", C.c_int64), ("factor_nnz", C.c_int64),
         ("forward_levels", C.c_int32), ("backward_levels", C.c_int32),
         ("factorize_count", C.c_int32), ("analyze_count", C.c_int32), ("device_bytes", C.c_int64),
-        ("cluster_ctas", C.c_int32), ("solve_kind", C.c_int32),
+        ("cluster_ctas", C.c_int32), ("solve_kind", C.c_int32), ("host_state", C.c_int32),
     ]
 
 
@@ -124,6 +127,8 @@ _SIGS = {
     "pd_sim_get_state": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
     "pd_sim_set_state": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
     "pd_sim_device_state": ([C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)], C.c_int),
+    "pd_sim_bind_host": ([C.c_void_p, C.POINTER(_dp), C.POINTER(_dp)], C.c_int),
+    "pd_sim_step_host": ([C.c_void_p, C.c_int32], C.c_int),
     "pd_sim_set_pin_positions": ([C.c_void_p, C.c_int32, _dp], C.c_int),
     "pd_sim_set_edge_stiffness": ([C.c_void_p, C.c_int32, _dp], C.c_int),
     "pd_sim_set_pinned": ([C.c_void_p, C.c_int32, _u8p, _dp], C.c_int),
@@ -399,6 +404,33 @@ class Simulator:
         vs = None if v is None else np.ascontiguousarray(v, np.float64)
         _check(self._lib.pd_sim_set_state(self._h, i, _ptr(xs, C.c_double), _ptr(vs, C.c_double)))
         self._keep = (xs, vs)  # host memory must outlive the queued copy
+
+    def bind_host(self, xs, vs):
+        """Binds one positions and one velocities array ((n, 3) contiguous float64) per instance for
+        step_host; None, None unbinds. Arrays in page-locked memory (e.g. numpy views of pinned
+        torch tensors) are moved by kernels inside one CUDA graph; they are kept referenced here."""
+        if xs is None and vs is None:
+            _check(self._lib.pd_sim_bind_host(self._h, None, None))
+            self._host = None
+            return
+        if isinstance(xs, np.ndarray):
+            xs, vs = [xs], [vs]
+        if len(xs) != self.count or len(vs) != self.count:
+            raise ValueError("one positions and one velocities array per instance")
+        for i, (x, v) in enumerate(zip(xs, vs)):
+            for a in (x, v):
+                if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != 3 * self.n[i]:
+                    raise ValueError("host state arrays must be contiguous float64 of shape (n, 3)")
+        px = (_dp * self.count)(*[_ptr(x, C.c_double) for x in xs])
+        pv = (_dp * self.count)(*[_ptr(v, C.c_double) for v in vs])
+        _check(self._lib.pd_sim_bind_host(self._h, px, pv))
+        self._host = (list(xs), list(vs))
+
+    def step_host(self, substeps: int = 1):
+        """Copies the bound arrays in, runs `substeps` substeps and copies them back (blocking)."""
+        _check(self._lib.pd_sim_step_host(self._h, int(substeps)))
+        if substeps > 0:
+            self._last = int(substeps)
 
     def device_state(self, i: int = 0):
         x, v = C.c_void_p(), C.c_void_p()

@@ -28,6 +28,7 @@ UNITS = {
     "substep_corr.cu": [],
     "adjoint.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
+    "state_copy.cu": [],
 }
 
 

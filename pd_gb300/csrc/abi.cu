@@ -575,12 +575,35 @@ struct pd_sim {
   int corrBig = 0;     // batch: instances (first in dDescOrder) run by clusters of kBatchCluster CTAs
   cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
   cudaEvent_t forkEv = nullptr, joinEv = nullptr;
+  unsigned generation = 0;      // bumped whenever the arena, the descriptors or the plan change
+  // host-state stepping (pd_sim_bind_host / pd_sim_step_host)
+  std::vector<double*> hostX, hostV;          // the caller's arrays, 3n doubles each
+  std::vector<pdg::HostStateDev> hostTable;   // device-visible addresses; empty unless all are page-locked
+  pdg::HostStateDev* dHostTable = nullptr;
+  unsigned tableGen = ~0u;
+  int* dNonFinite = nullptr;                  // set by the gather on a non-finite position
+  int* hNonFinite = nullptr;                  // its page-locked copy, read after the step
+  cudaGraphExec_t graphExec = nullptr;        // gather → substeps → scatter, replayed per call
+  int graphSubsteps = -1;
+  unsigned graphGen = ~0u;
+  cudaStream_t ownStream = nullptr;           // capture stream when the handle's stream is the default
 
   ~pd_sim() {
     release();
     if (aux) cudaStreamDestroy(aux);
     if (forkEv) cudaEventDestroy(forkEv);
     if (joinEv) cudaEventDestroy(joinEv);
+    dropGraph();
+    if (dHostTable) cudaFree(dHostTable);
+    if (dNonFinite) cudaFree(dNonFinite);
+    if (hNonFinite) cudaFreeHost(hNonFinite);
+    if (ownStream) cudaStreamDestroy(ownStream);
+  }
+  void dropGraph() {
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    graphExec = nullptr;
+    graphSubsteps = -1;
+    graphGen = ~0u;
   }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
 
@@ -756,6 +779,7 @@ struct pd_sim {
   }
 
   int writeDescriptors() {
+    ++generation;
     std::vector<pdg::InstanceDev> desc;
     int smem = 0;
     // over-relaxation weights, one table per instance
@@ -856,6 +880,86 @@ struct pd_sim {
       PD_CUDA(cudaMemcpy(I.scene.x.data(), dArena + I.oX, 24 * I.scene.n, cudaMemcpyDeviceToHost));
       PD_CUDA(cudaMemcpy(I.scene.v.data(), dArena + I.oV, 24 * I.scene.n, cudaMemcpyDeviceToHost));
     }
+    return PD_OK;
+  }
+
+  // The second stream and its fork/join events, created before any launch (or capture) needs them.
+  int ensureAux() {
+    if (corrBig <= 0 || aux) return PD_OK;
+    PD_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+    PD_CUDA(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
+    PD_CUDA(cudaEventCreateWithFlags(&joinEv, cudaEventDisableTiming));
+    return PD_OK;
+  }
+
+  // Queues `substeps` substeps of every instance on `st`: the residual-trace reset, then the
+  // planned kernel (for a MIXED batch with large cloths: their clusters on the second stream
+  // beside the one-CTA launch of the rest). Logs and the second stream must already exist.
+  int launchSubsteps(cudaStream_t st, int substeps) {
+    const int count = static_cast<int>(inst.size());
+    if (traceOn && traceLen) PD_CUDA(cudaMemsetAsync(dTrace, 0xFF, sizeof(double) * traceLen, st));
+    int rc;
+    const int p = precision();
+    if (p == PD_PRECISION_FP64_EXACT) {
+      rc = pdg::launchSubstepExact(dDesc, count, substeps, smemBytes, st);
+    } else if (delta) {
+      rc = pdg::launchSubstepDelta(dDesc, count, teamCtas, smemBytes, substeps, st);
+    } else if (corr) {
+      if (teamCtas > 1) {
+        rc = pdg::launchSubstepCorrCluster(dDesc, count, teamCtas, substeps, st);
+      } else if (corrBig > 0) {  // large cloths in clusters on the second stream, the rest here
+        PD_CUDA(cudaEventRecord(forkEv, st));
+        PD_CUDA(cudaStreamWaitEvent(aux, forkEv, 0));
+        rc = pdg::launchSubstepCorrCluster(dDescOrder, corrBig, kBatchCluster, substeps, aux);
+        if (rc == 0) rc = pdg::launchSubstepCorr(dDescOrder + corrBig, count - corrBig, substeps, smemBytes, st);
+        if (rc == 0) {
+          PD_CUDA(cudaEventRecord(joinEv, aux));
+          PD_CUDA(cudaStreamWaitEvent(st, joinEv, 0));
+        }
+      } else {
+        rc = pdg::launchSubstepCorr(dDescOrder ? dDescOrder : dDesc, count, substeps, smemBytes, st);
+      }
+    } else if (dense) {
+      rc = pdg::launchSubstepDenseCluster(dDesc, count, teamCtas, smemBytes, substeps, st);
+    } else if (mixedSolve(p)) {
+      rc = teamCtas > 1 ? pdg::launchSubstepMixedCluster(dDesc, count, teamCtas, smemBytes, substeps, st)
+                        : pdg::launchSubstepMixed(dDesc, count, substeps, smemBytes, st);
+    } else {
+      rc = teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st)
+                        : pdg::launchSubstepFast(dDesc, count, substeps, smemBytes, st);
+    }
+    if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
+    return PD_OK;
+  }
+
+  // Records gather → substeps → scatter → copy of the non-finite flag on `st` as a CUDA graph.
+  int captureHostStep(cudaStream_t st, int substeps) {
+    dropGraph();
+    const int count = static_cast<int>(inst.size());
+    int maxN = 1;
+    for (const auto& I : inst) maxN = std::max(maxN, I.scene.n);
+    PD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = PD_OK;
+    cudaError_t e = cudaMemsetAsync(dNonFinite, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = static_cast<cudaError_t>(pdg::launchGatherState(dHostTable, count, maxN, dNonFinite, st));
+    if (e == cudaSuccess && substeps > 0) rc = launchSubsteps(st, substeps);
+    if (e == cudaSuccess && rc == PD_OK) e = static_cast<cudaError_t>(pdg::launchScatterState(dHostTable, count, maxN, st));
+    if (e == cudaSuccess && rc == PD_OK) e = cudaMemcpyAsync(hNonFinite, dNonFinite, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(st, &g);
+    if (rc == PD_OK && (e != cudaSuccess || ee != cudaSuccess))
+      rc = cudaFail(e != cudaSuccess ? e : ee, "capture of the host-state step");
+    if (rc == PD_OK) {
+      e = cudaGraphInstantiate(&graphExec, g, 0);
+      if (e != cudaSuccess) {
+        graphExec = nullptr;
+        rc = cudaFail(e, "cudaGraphInstantiate of the host-state step");
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+    if (rc != PD_OK) return rc;
+    graphSubsteps = substeps;
+    graphGen = generation;
     return PD_OK;
   }
 };
@@ -1148,47 +1252,9 @@ int pd_sim_step(pd_sim* s, int32_t substeps) {
     const int rc = s->ensureLogs(substeps);
     if (rc != PD_OK) return rc;
   }
-  const int count = static_cast<int>(s->inst.size());
-  if (s->traceOn && s->traceLen) PD_CUDA(cudaMemsetAsync(s->dTrace, 0xFF, sizeof(double) * s->traceLen, s->stream));
-  int rc;
-  const int p = s->precision();
-  if (p == PD_PRECISION_FP64_EXACT) {
-    rc = pdg::launchSubstepExact(s->dDesc, count, substeps, s->smemBytes, s->stream);
-  } else if (s->delta) {
-    rc = pdg::launchSubstepDelta(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
-  } else if (s->corr) {
-    if (s->teamCtas > 1) {
-      rc = pdg::launchSubstepCorrCluster(s->dDesc, count, s->teamCtas, substeps, s->stream);
-    } else if (s->corrBig > 0) {  // large cloths in clusters on the second stream, the rest here
-      if (!s->aux) {
-        PD_CUDA(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
-        PD_CUDA(cudaEventCreateWithFlags(&s->forkEv, cudaEventDisableTiming));
-        PD_CUDA(cudaEventCreateWithFlags(&s->joinEv, cudaEventDisableTiming));
-      }
-      PD_CUDA(cudaEventRecord(s->forkEv, s->stream));
-      PD_CUDA(cudaStreamWaitEvent(s->aux, s->forkEv, 0));
-      rc = pdg::launchSubstepCorrCluster(s->dDescOrder, s->corrBig, kBatchCluster, substeps, s->aux);
-      if (rc == 0)
-        rc = pdg::launchSubstepCorr(s->dDescOrder + s->corrBig, count - s->corrBig, substeps, s->smemBytes,
-                                    s->stream);
-      if (rc == 0) {
-        PD_CUDA(cudaEventRecord(s->joinEv, s->aux));
-        PD_CUDA(cudaStreamWaitEvent(s->stream, s->joinEv, 0));
-      }
-    } else {
-      rc = pdg::launchSubstepCorr(s->dDescOrder ? s->dDescOrder : s->dDesc, count, substeps, s->smemBytes,
-                                  s->stream);
-    }
-  } else if (s->dense) {
-    rc = pdg::launchSubstepDenseCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream);
-  } else if (mixedSolve(p)) {
-    rc = s->teamCtas > 1 ? pdg::launchSubstepMixedCluster(s->dDesc, count, s->teamCtas, s->smemBytes, substeps, s->stream)
-                         : pdg::launchSubstepMixed(s->dDesc, count, substeps, s->smemBytes, s->stream);
-  } else {
-    rc = s->teamCtas > 1 ? pdg::launchSubstepCluster(s->dDesc, count, s->teamCtas, substeps, s->stream)
-                         : pdg::launchSubstepFast(s->dDesc, count, substeps, s->smemBytes, s->stream);
-  }
-  if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
+  int rc = s->ensureAux();
+  if (rc == PD_OK) rc = s->launchSubsteps(s->stream, substeps);
+  if (rc != PD_OK) return rc;
   s->lastSubsteps = substeps;
   return PD_OK;
 }
@@ -1227,6 +1293,120 @@ int pd_sim_set_state(pd_sim* s, int32_t i, const double* x, const double* v) {
     PD_CUDA(cudaMemcpyAsync(s->dArena + I.oX, x, bytes, cudaMemcpyHostToDevice, s->stream));
   }
   if (v) PD_CUDA(cudaMemcpyAsync(s->dArena + I.oV, v, bytes, cudaMemcpyHostToDevice, s->stream));
+  return PD_OK;
+}
+
+// Device-visible address of `count` doubles at host address p if the whole range lies in one
+// page-locked (cudaHostAlloc / cudaHostRegister) allocation, else null.
+static double* mappedHost(double* p, size_t count) {
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  double* last = p + (count - 1);
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  double* d = static_cast<double*>(a.devicePointer);
+  if (b.type != cudaMemoryTypeHost || static_cast<double*>(b.devicePointer) != d + (count - 1)) return nullptr;
+  return d;
+}
+
+int pd_sim_bind_host(pd_sim* s, double* const* x, double* const* v) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (const int rc_ = s->sync()) return rc_;  // no launch in flight still reads the old arrays
+  s->dropGraph();
+  s->hostX.clear();
+  s->hostV.clear();
+  s->hostTable.clear();
+  s->tableGen = ~0u;
+  if (!x && !v) return PD_OK;  // unbind
+  if (!x || !v) return fail(PD_ERR_INVALID_ARGUMENT, "positions and velocities must both be given");
+  const size_t count = s->inst.size();
+  for (size_t i = 0; i < count; ++i)
+    if (!x[i] || !v[i]) return fail(PD_ERR_INVALID_ARGUMENT, "instance " + std::to_string(i) + ": null array");
+  std::vector<pdg::HostStateDev> table(count);
+  bool mapped = count <= 65535;
+  for (size_t i = 0; i < count && mapped; ++i) {
+    const size_t n3 = 3 * static_cast<size_t>(s->inst[i].scene.n);
+    table[i].hx = mappedHost(x[i], n3);
+    table[i].hv = mappedHost(v[i], n3);
+    table[i].n = s->inst[i].scene.n;
+    mapped = table[i].hx && table[i].hv;
+  }
+  s->hostX.assign(x, x + count);
+  s->hostV.assign(v, v + count);
+  if (mapped) s->hostTable = std::move(table);
+  return PD_OK;
+}
+
+int pd_sim_step_host(pd_sim* s, int32_t substeps) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (substeps < 0) return fail(PD_ERR_INVALID_ARGUMENT, "substeps must be >= 0");
+  if (s->hostX.empty()) return fail(PD_ERR_STATE, "no host arrays are bound (pd_sim_bind_host)");
+  if (substeps > s->logCapacity) {
+    if (const int rc_ = s->sync()) return rc_;
+    const int rc = s->ensureLogs(substeps);
+    if (rc != PD_OK) return rc;
+  }
+  if (const int rc = s->ensureAux()) return rc;
+  const size_t count = s->inst.size();
+  if (s->hostTable.empty()) {  // pageable arrays: one copy per array each way
+    for (size_t i = 0; i < count; ++i) {
+      const size_t n3 = 3 * static_cast<size_t>(s->inst[i].scene.n);
+      for (size_t k = 0; k < n3; ++k)
+        if (!std::isfinite(s->hostX[i][k])) return fail(PD_ERR_INVALID_ARGUMENT, "positions contain a non-finite value");
+    }
+    for (size_t i = 0; i < count; ++i) {
+      const Instance& I = s->inst[i];
+      const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
+      PD_CUDA(cudaMemcpyAsync(s->dArena + I.oX, s->hostX[i], bytes, cudaMemcpyHostToDevice, s->stream));
+      PD_CUDA(cudaMemcpyAsync(s->dArena + I.oV, s->hostV[i], bytes, cudaMemcpyHostToDevice, s->stream));
+    }
+    if (substeps > 0) {
+      if (const int rc = s->launchSubsteps(s->stream, substeps)) return rc;
+      s->lastSubsteps = substeps;
+    }
+    for (size_t i = 0; i < count; ++i) {
+      const Instance& I = s->inst[i];
+      const size_t bytes = 24 * static_cast<size_t>(I.scene.n);
+      PD_CUDA(cudaMemcpyAsync(s->hostX[i], s->dArena + I.oX, bytes, cudaMemcpyDeviceToHost, s->stream));
+      PD_CUDA(cudaMemcpyAsync(s->hostV[i], s->dArena + I.oV, bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
+    return s->sync();
+  }
+  // page-locked arrays: gather kernel → substeps → scatter kernel, one CUDA graph replay
+  cudaStream_t st = s->stream;
+  if (!st) {  // a graph cannot be captured on the legacy default stream
+    if (!s->ownStream) PD_CUDA(cudaStreamCreate(&s->ownStream));
+    st = s->ownStream;
+  }
+  if (s->tableGen != s->generation) {
+    for (size_t i = 0; i < count; ++i) {
+      s->hostTable[i].dx = reinterpret_cast<double*>(s->dArena + s->inst[i].oX);
+      s->hostTable[i].dv = reinterpret_cast<double*>(s->dArena + s->inst[i].oV);
+    }
+    if (!s->dHostTable) PD_CUDA(cudaMalloc(&s->dHostTable, sizeof(pdg::HostStateDev) * count));
+    PD_CUDA(cudaMemcpy(s->dHostTable, s->hostTable.data(), sizeof(pdg::HostStateDev) * count,
+                       cudaMemcpyHostToDevice));
+    s->tableGen = s->generation;
+  }
+  if (!s->dNonFinite) {
+    PD_CUDA(cudaMalloc(&s->dNonFinite, sizeof(int)));
+    PD_CUDA(cudaHostAlloc(&s->hNonFinite, sizeof(int), cudaHostAllocDefault));
+  }
+  if (!s->graphExec || s->graphSubsteps != substeps || s->graphGen != s->generation)
+    if (const int rc = s->captureHostStep(st, substeps)) return rc;
+  *s->hNonFinite = 0;
+  PD_CUDA(cudaGraphLaunch(s->graphExec, st));
+  if (substeps > 0) s->lastSubsteps = substeps;
+  if (st != s->stream) PD_CUDA(cudaStreamSynchronize(st));
+  if (const int rc_ = s->sync()) return rc_;
+  if (*s->hNonFinite)
+    return fail(PD_ERR_INVALID_ARGUMENT, "a bound position array holds a non-finite value (the step ran on it)");
   return PD_OK;
 }
 
@@ -1339,6 +1519,8 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   out->analyze_count = I.analyzeCount;
   out->device_bytes = static_cast<int64_t>(I.bytes);
   out->cluster_ctas = (s->corr && I.corrTeam > 1) ? I.corrTeam : s->teamCtas;
+  out->host_state = s->hostX.empty() ? PD_HOST_STATE_NONE : s->hostTable.empty() ? PD_HOST_STATE_COPIES
+                                                                                 : PD_HOST_STATE_GRAPH;
   const int p = s->precision();
   out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                     : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
@@ -1579,6 +1761,7 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
     Arena A;
     layout(I, A, 1, 0);
     info->cluster_ctas = 1;
+    info->host_state = PD_HOST_STATE_NONE;
     info->solve_kind = I.cfg.precision == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                        : mixedSolve(I.cfg.precision)              ? PD_SOLVE_SUPERNODAL32
                                                                   : PD_SOLVE_SUPERNODAL;

@@ -200,7 +200,22 @@ int gradClusterSupported(int clusterSize);
 // columns per CTA, one in each component of the solve.
 int launchDenseInverse(const InstanceDev* dInstance, int n, void* stream);
 
-constexpr int kBlockThreads = 256;    // one CTA per cloth (several CTAs share an SM in a batch), and
+// One instance's state in the caller's page-locked host arrays (device-visible addresses) and in
+// the arena (state_copy.cu).
+struct HostStateDev {
+  double* hx;
+  double* hv;
+  double* dx;
+  double* dv;
+  int32_t n;
+};
+// Host → arena for every instance (grid: chunks × instances, count ≤ 65535); sets *dNonFinite
+// when a position is not finite. maxN: the largest instance's vertex count.
+int launchGatherState(const HostStateDev* dTable, int count, int maxN, int* dNonFinite, void* stream);
+// Arena → host for every instance.
+int launchScatterState(const HostStateDev* dTable, int count, int maxN, void* stream);
+
+constexpr int kBlockThreads = 256;   // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per
                                       // barrier beat more threads per level there)
 constexpr int kClusterThreads = 1024; // mixed cluster kernels: one CTA fills its SM to hide L2 latency
