@@ -76,6 +76,7 @@ def parse():
     p.add_argument("--no-pos-err", action="store_true")
     p.add_argument("--no-fp64-gpu", action="store_true")
     p.add_argument("--no-cheb", action="store_true")
+    p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--grad-side", type=int, default=64)         # smaller only for profiling captures
@@ -283,6 +284,8 @@ def time_fp64_gpu(P, args, stream, flush, max_steps=10):
     scenes, cfgs, _ = workload(args.workload, args.batch_count, "fp64")
     sim = P.Simulator(scenes, cfgs)
     sim.set_stream(stream.cuda_stream)
+    if not args.no_autotune:  # the baseline gets the same autotuner
+        sim.autotune(5)
     k = min(args.steps, max_steps)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
@@ -298,7 +301,7 @@ def time_fp64_gpu(P, args, stream, flush, max_steps=10):
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / k
     return {"value": len(scenes) * 1e3 / ms, "unit": UNIT, "steps": k, "kernel": kernel_name(sim.info(0)),
-            "ctas_per_cloth": sim.info(0)["cluster_ctas"]}
+            "ctas_per_cloth": sim.info(0)["cluster_ctas"], "plan": sim.plan()}
 
 
 def chebyshev_line(P, args, stream, flush, max_steps=100):
@@ -362,17 +365,24 @@ def time_fp64_one_at_a_time(P, args, budget_s=120.0):
             "how": "one cloth per launch, plain FP64 path, per-cloth launch times summed"}
 
 
-def position_error(P, args, scenes, cfgs, substeps):
-    """max |x_gpu − x_oracle| / max |x_oracle| of cloth 0 after `substeps` substeps from the
-    initial state, this precision mode against the FP64 CPU oracle."""
+def position_error(P, args, scenes, cfgs, substeps, plan=None):
+    """max |x_gpu − x_oracle| / max |x_oracle| after `substeps` substeps from the initial state, this
+    precision mode against the FP64 CPU oracle, for the run as timed: every cloth on one handle with
+    the timed launch plan; checked on cloth 0 and on the largest cloth."""
     from tests.helpers import max_rel, oracle_twin  # checker only
-    sim = P.Simulator([scenes[0]], [cfgs[0]])
-    orc = oracle_twin(scenes[0], cfgs[0], perm=sim.factor(0)["perm"], threads=os.cpu_count())
+    sim = P.Simulator(scenes, cfgs)
+    if plan is not None:
+        sim.set_plan(plan)
     sim.step(substeps)
-    orc.step(substeps)
-    err = max_rel(sim.state(0)[0], orc.state()[0])
+    picks = sorted({0, int(np.argmax([sc.n for sc in scenes]))})
+    errs = {}
+    for i in picks:
+        orc = oracle_twin(scenes[i], cfgs[i], perm=sim.factor(i)["perm"], threads=os.cpu_count())
+        orc.step(substeps)
+        errs[str(i)] = max_rel(sim.state(i)[0], orc.state()[0])
+    err = max(errs.values())
     return {"value": err, "bound": POS_ERR_BOUND, "within": bool(err <= POS_ERR_BOUND), "substeps": substeps,
-            "against": "FP64 CPU oracle (reference algorithm restated), cloth 0"}
+            "cloths": errs, "against": "FP64 CPU oracle (reference algorithm restated), cloths of the run as timed"}
 
 
 def run_ours(args):
@@ -388,6 +398,15 @@ def run_ours(args):
     sim = P.Simulator(scenes, cfgs)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
+    # launch plan: the autotuner times candidates on this workload (outside every timed region)
+    tune = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        rep = sim.autotune(3 if len(scenes) > 1 else 20)
+        tune = {"candidates": len(rep["tried"]), "chosen": rep["tried"][rep["chosen"]],
+                "chosen_ms": rep["ms"][rep["chosen"]], "builtin_ms": rep["ms"][0],
+                "seconds": time.perf_counter() - t0}
+    plan = sim.plan()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -463,7 +482,7 @@ def run_ours(args):
             fp64_line = (time_fp64_one_at_a_time(P, args) if len(scenes) > 1
                          else time_fp64_gpu(P, args, stream, flush))
         if not args.no_pos_err:
-            pos_err = position_error(P, args, scenes, cfgs, sub)
+            pos_err = position_error(P, args, scenes, cfgs, sub, plan)
 
     if rank == 0:
         info = sim.info(0)
@@ -489,7 +508,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "pd_sim_step_host (gather kernel, substep, scatter kernel: one CUDA graph)"
                         if info["host_state"] == P.PD_HOST_STATE_GRAPH else "pd_sim_step_host (cudaMemcpyAsync per array)"},
-                "clocks": clocks}
+                "clocks": clocks, "plan": plan, "autotune": tune}
         if PRECISIONS[args.precision][0] <= 1:
             ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
             fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU

@@ -251,6 +251,40 @@ int pd_sim_device_state(pd_sim* s, int32_t instance, double** positions, double*
  * The handle's stream orders the work; on the default stream a private stream carries the graph. */
 int pd_sim_bind_host(pd_sim* s, double* const* positions, double* const* velocities);
 int pd_sim_step_host(pd_sim* s, int32_t substeps);
+
+/* ---- Launch plan and autotuner (the north star's "level-group and tile sizes chosen by an
+ * autotuner"; no counterpart in the reference, whose solve runs on host threads) ----
+ * A plan overrides the planner's built-in choices; 0 keeps the built-in choice of a field. */
+typedef struct pd_plan {
+  int32_t team_ctas;         /* CTAs per cloth: the MIXED team kernel's team, or the thread-block
+                                cluster of the supernodal kernels (takes precedence over
+                                pd_scene_config.cluster_ctas) */
+  int32_t big_min_vertices;  /* MIXED batches above the explicit-inverse limit: cloths of at least
+                                this many vertices run as clusters on a second stream (built-in
+                                8192; < 0: none) */
+  int32_t big_cluster_ctas;  /* CTAs of each of those clusters (built-in 4) */
+  double latency_scale;      /* weight of the dependent-latency term against the issue term in the
+                                lanes-per-row model of every supernodal level (built-in 1) */
+} pd_plan;
+
+#define PD_TUNE_MAX_CANDIDATES 32
+/* Times candidate plans for this handle's own workload and keeps the fastest: the team size of
+ * the team kernel; the large-cloth threshold and cluster size of a batch; the CTAs per cloth of a
+ * supernodal kernel; then the latency weight of the lane model for the best of those. Each
+ * candidate is re-planned and re-uploaded, starts from the handle's current state, runs one
+ * warm-up substep and then `substeps` timed substeps (CUDA events on the handle's stream). The
+ * state, pin targets and counters are restored afterwards, so tuning does not advance the
+ * simulation; the per-substep iteration logs and residual trace are cleared. FP64_EXACT keeps its
+ * reference order: one candidate. Results of different plans differ only in rounding (the sums
+ * of a row are split over other lane counts), each plan bit-reproducible. tried / ms_per_substep
+ * receive up to PD_TUNE_MAX_CANDIDATES entries (nullable): the effective plan of each candidate
+ * (the planner's choices filled in) and its time; *chosen indexes the kept one (candidate 0 is
+ * the built-in plan). */
+int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_substep, int32_t* n_tried,
+                    int32_t* chosen);
+/* Applies a plan (re-plans and re-uploads; the state is kept) / reads the effective plan. */
+int pd_sim_set_plan(pd_sim* s, const pd_plan* plan);
+int pd_sim_get_plan(pd_sim* s, pd_plan* out);
 /* Moves pin targets; only the RHS changes, no refactorization (core/assemble/Assembler.h:52-60). */
 int pd_sim_set_pin_positions(pd_sim* s, int32_t instance, const double* pin_positions);
 /* Changes edge stiffnesses; refactorizes (the stamp changes, Assembler.cpp:111-147). */

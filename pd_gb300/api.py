@@ -83,6 +83,14 @@ class _SimInfo(C.Structure):
     ]
 
 
+class _Plan(C.Structure):
+    _fields_ = [("team_ctas", C.c_int32), ("big_min_vertices", C.c_int32), ("big_cluster_ctas", C.c_int32),
+                ("latency_scale", C.c_double)]
+
+
+PD_TUNE_MAX_CANDIDATES = 32
+
+
 class _SimStats(C.Structure):
     _fields_ = [("iterations_used", C.c_int32), ("converged", C.c_int32),
                 ("early_exit_count", C.c_int32), ("last_residual", C.c_double)]
@@ -128,6 +136,9 @@ _SIGS = {
     "pd_sim_set_state": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
     "pd_sim_device_state": ([C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)], C.c_int),
     "pd_sim_bind_host": ([C.c_void_p, C.POINTER(_dp), C.POINTER(_dp)], C.c_int),
+    "pd_sim_autotune": ([C.c_void_p, C.c_int32, C.POINTER(_Plan), _dp, _ip, _ip], C.c_int),
+    "pd_sim_set_plan": ([C.c_void_p, C.POINTER(_Plan)], C.c_int),
+    "pd_sim_get_plan": ([C.c_void_p, C.POINTER(_Plan)], C.c_int),
     "pd_sim_step_host": ([C.c_void_p, C.c_int32], C.c_int),
     "pd_sim_set_pin_positions": ([C.c_void_p, C.c_int32, _dp], C.c_int),
     "pd_sim_set_edge_stiffness": ([C.c_void_p, C.c_int32, _dp], C.c_int),
@@ -431,6 +442,27 @@ class Simulator:
         _check(self._lib.pd_sim_step_host(self._h, int(substeps)))
         if substeps > 0:
             self._last = int(substeps)
+
+    def autotune(self, substeps: int = 10) -> dict:
+        """Times candidate launch plans on this batch and keeps the fastest (pd_sim_autotune); the
+        simulation state is unchanged. Returns {"tried": [plan dicts], "ms": [...], "chosen": k}."""
+        plans = (_Plan * PD_TUNE_MAX_CANDIDATES)()
+        ms = np.zeros(PD_TUNE_MAX_CANDIDATES)
+        n, k = C.c_int32(), C.c_int32()
+        _check(self._lib.pd_sim_autotune(self._h, int(substeps), plans, _ptr(ms, C.c_double), C.byref(n), C.byref(k)))
+        tried = [{f: getattr(plans[i], f) for f, _ in _Plan._fields_} for i in range(n.value)]
+        self._last = 0
+        return {"tried": tried, "ms": ms[:n.value].tolist(), "chosen": k.value}
+
+    def plan(self) -> dict:
+        p = _Plan()
+        _check(self._lib.pd_sim_get_plan(self._h, C.byref(p)))
+        return {f: getattr(p, f) for f, _ in _Plan._fields_}
+
+    def set_plan(self, plan: dict):
+        p = _Plan(**{f: plan.get(f, 0) for f, _ in _Plan._fields_})
+        _check(self._lib.pd_sim_set_plan(self._h, C.byref(p)))
+        self._last = 0
 
     def device_state(self, i: int = 0):
         x, v = C.c_void_p(), C.c_void_p()

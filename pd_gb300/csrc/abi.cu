@@ -225,10 +225,10 @@ int deltaSmem(const Instance& I, int team, int* resRows) {
 
 // kind: 0 none, 1 dense inverse (cluster kernel), 2 dense inverse + team kernel buffers,
 // 3 FP32 tables + position pairs of the one-CTA correction kernel
-void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
+void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencyScale = 1.0) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
-  I.oLvlG = A.add(pdg::chooseGroupWidths(I.F, teamCtas));
+  I.oLvlG = A.add(pdg::chooseGroupWidths(I.F, teamCtas, latencyScale));
   const size_t before = A.host.size();
   I.denseLd = 0;
   I.denseResRows = 0;
@@ -363,9 +363,10 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind) {
   I.oInvLT = A.add(I.F.invLT);
   I.oT = A.zeros(24 * n);
   // FP32 solve: the correction kernel's teams are 256-thread CTAs, the other mixed kernels' 1024
-  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam)
+  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam, latencyScale)
                                    : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
-                                                                                : pdg::kBlockThreads));
+                                                                                : pdg::kBlockThreads,
+                                                              1, latencyScale));
   I.oLrv32 = A.add(I.F.rowval32);
   I.oLcv32 = A.add(I.F.colval32);
   I.oInvL32 = A.add(I.F.invL32);
@@ -576,6 +577,8 @@ struct pd_sim {
   cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
   cudaEvent_t forkEv = nullptr, joinEv = nullptr;
   unsigned generation = 0;      // bumped whenever the arena, the descriptors or the plan change
+  pd_plan plan{};               // overrides of the planner's choices (pd_sim_set_plan / pd_sim_autotune)
+  int bigCs = kBatchCluster;    // CTAs per large cloth of a MIXED batch on the second stream
   // host-state stepping (pd_sim_bind_host / pd_sim_step_host)
   std::vector<double*> hostX, hostV;          // the caller's arrays, 3n doubles each
   std::vector<pdg::HostStateDev> hostTable;   // device-visible addresses; empty unless all are page-locked
@@ -606,6 +609,9 @@ struct pd_sim {
     graphGen = ~0u;
   }
   int precision() const { return inst.empty() ? PD_PRECISION_FP64_EXACT : inst[0].cfg.precision; }
+  double latencyScale() const { return plan.latency_scale > 0.0 ? plan.latency_scale : 1.0; }
+  // CTAs per cloth the caller asked for: the plan's, else the configuration's (0: the planner's)
+  int wantCtas() const { return plan.team_ctas > 0 ? plan.team_ctas : inst[0].cfg.cluster_ctas; }
 
   // CTAs per cloth for the supernodal FP64 kernel: the requested count, or 16 for up to nine
   // cloths (152 SMs / 16) and fewer for larger batches; reduced until the device accepts it.
@@ -630,23 +636,27 @@ struct pd_sim {
         teamCtas = planCorr();
         if (teamCtas > 1) {
           for (auto& I : inst) I.corrTeam = teamCtas;
-        } else if (inst.size() > 1 && pdg::corrClusterSupported(kBatchCluster) == kBatchCluster) {
+        } else if (inst.size() > 1 && plan.big_min_vertices >= 0 &&
+                   pdg::corrClusterSupported(bigCs = plan.big_cluster_ctas > 0 ? plan.big_cluster_ctas
+                                                                               : kBatchCluster) == bigCs) {
           // a batch: the large cloths, whose one-CTA time would set the launch's makespan, get a
           // small cluster each and run on a second stream beside the others
+          const int bigMin = plan.big_min_vertices > 0 ? plan.big_min_vertices : kBatchClusterMinVertices;
           for (auto& I : inst)
-            if (I.scene.n >= kBatchClusterMinVertices) {
-              I.corrTeam = kBatchCluster;
+            if (I.scene.n >= bigMin) {
+              I.corrTeam = bigCs;
               ++corrBig;
             }
           if (corrBig == static_cast<int>(inst.size())) {  // all large: one clustered launch
-            teamCtas = kBatchCluster;
+            teamCtas = bigCs;
+            for (auto& I : inst) I.corrTeam = bigCs;
             corrBig = 0;
           }
         }
       }
       return;
     }
-    int want = inst[0].cfg.cluster_ctas;
+    int want = wantCtas();
     if (want <= 0) {
       const int count = static_cast<int>(inst.size());
       want = count <= 9 ? 16 : count <= 19 ? 8 : count <= 38 ? 4 : count <= 76 ? 2 : 1;
@@ -689,7 +699,7 @@ struct pd_sim {
       return false;
     }
     const int count = static_cast<int>(inst.size());
-    const int want = inst[0].cfg.cluster_ctas;
+    const int want = wantCtas();
     int team = want > 0 ? want : sms / count;
     team = std::min({team, sms / count, minN, 256});  // 256: partials one polling warp covers
     if (team < 2) return false;
@@ -703,7 +713,7 @@ struct pd_sim {
   // CTAs per cloth of the correction kernel: a cluster for a few large cloths (as for the FP64
   // supernodal kernel), one CTA per cloth for batches and small cloths.
   int planCorr() const {
-    int want = inst[0].cfg.cluster_ctas;
+    int want = wantCtas();
     if (want <= 0) {
       int minN = 1 << 30;
       for (const auto& I : inst) minN = std::min(minN, I.scene.n);
@@ -747,7 +757,7 @@ struct pd_sim {
   int upload(int capacity) {
     Arena A;
     planTeam();
-    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : corr ? 3 : dense ? 1 : 0);
+    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : corr ? 3 : dense ? 1 : 0, latencyScale());
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -910,7 +920,7 @@ struct pd_sim {
       } else if (corrBig > 0) {  // large cloths in clusters on the second stream, the rest here
         PD_CUDA(cudaEventRecord(forkEv, st));
         PD_CUDA(cudaStreamWaitEvent(aux, forkEv, 0));
-        rc = pdg::launchSubstepCorrCluster(dDescOrder, corrBig, kBatchCluster, substeps, aux);
+        rc = pdg::launchSubstepCorrCluster(dDescOrder, corrBig, bigCs, substeps, aux);
         if (rc == 0) rc = pdg::launchSubstepCorr(dDescOrder + corrBig, count - corrBig, substeps, smemBytes, st);
         if (rc == 0) {
           PD_CUDA(cudaEventRecord(joinEv, aux));
@@ -1545,6 +1555,188 @@ int pd_sim_get_stats(pd_sim* s, int32_t i, pd_sim_stats* out) {
   out->iterations_used = ints[0];
   out->converged = ints[1];
   out->early_exit_count = ints[2];
+  return PD_OK;
+}
+
+// ------------------------------------------------------------------------------ plan / autotuner
+// State a re-plan must carry over: positions, velocities and the gate counters of every instance.
+struct SavedSim {
+  std::vector<std::vector<double>> x, v;
+  std::vector<double> lastRes;
+  std::vector<int32_t> iters, conv, early;
+};
+
+static int saveSim(pd_sim* s, SavedSim& o) {
+  if (const int rc = s->pullState()) return rc;
+  const size_t count = s->inst.size();
+  o.x.resize(count);
+  o.v.resize(count);
+  o.lastRes.resize(count);
+  o.iters.resize(count);
+  o.conv.resize(count);
+  o.early.resize(count);
+  for (size_t i = 0; i < count; ++i) {
+    const Instance& I = s->inst[i];
+    o.x[i] = I.scene.x;
+    o.v[i] = I.scene.v;
+    PD_CUDA(cudaMemcpy(&o.lastRes[i], s->dArena + I.oLastRes, sizeof(double), cudaMemcpyDeviceToHost));
+    PD_CUDA(cudaMemcpy(&o.iters[i], s->dArena + I.oIters, 4, cudaMemcpyDeviceToHost));
+    PD_CUDA(cudaMemcpy(&o.conv[i], s->dArena + I.oConv, 4, cudaMemcpyDeviceToHost));
+    PD_CUDA(cudaMemcpy(&o.early[i], s->dArena + I.oEarly, 4, cudaMemcpyDeviceToHost));
+  }
+  return PD_OK;
+}
+
+// Re-plans and re-uploads from the saved state (the arena is seeded from the host scenes).
+static int replan(pd_sim* s, const pd_plan& p, const SavedSim& o, int capacity) {
+  s->plan = p;
+  for (size_t i = 0; i < s->inst.size(); ++i) {
+    s->inst[i].scene.x = o.x[i];
+    s->inst[i].scene.v = o.v[i];
+  }
+  if (const int rc = s->upload(capacity)) return rc;
+  return s->ensureAux();
+}
+
+static int restoreCounters(pd_sim* s, const SavedSim& o) {
+  for (size_t i = 0; i < s->inst.size(); ++i) {
+    const Instance& I = s->inst[i];
+    PD_CUDA(cudaMemcpy(s->dArena + I.oLastRes, &o.lastRes[i], sizeof(double), cudaMemcpyHostToDevice));
+    PD_CUDA(cudaMemcpy(s->dArena + I.oIters, &o.iters[i], 4, cudaMemcpyHostToDevice));
+    PD_CUDA(cudaMemcpy(s->dArena + I.oConv, &o.conv[i], 4, cudaMemcpyHostToDevice));
+    PD_CUDA(cudaMemcpy(s->dArena + I.oEarly, &o.early[i], 4, cudaMemcpyHostToDevice));
+  }
+  s->lastSubsteps = 0;  // the logs and trace of the tuning launches are not the simulation's
+  return PD_OK;
+}
+
+static pd_plan effectivePlan(const pd_sim* s) {
+  pd_plan p{};
+  p.team_ctas = s->teamCtas;
+  p.big_min_vertices = s->plan.big_min_vertices != 0 ? s->plan.big_min_vertices : kBatchClusterMinVertices;
+  p.big_cluster_ctas = s->bigCs;
+  p.latency_scale = s->latencyScale();
+  return p;
+}
+
+// Mean time of one substep over `substeps` substeps after one warm-up substep.
+static int timeSubsteps(pd_sim* s, int substeps, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+  if (const int rc = s->launchSubsteps(s->stream, 1)) return rc;
+  PD_CUDA(cudaEventRecord(e0, s->stream));
+  if (const int rc = s->launchSubsteps(s->stream, substeps)) return rc;
+  PD_CUDA(cudaEventRecord(e1, s->stream));
+  if (const int rc = s->sync()) return rc;
+  float t = 0.f;
+  PD_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  *ms = static_cast<double>(t) / substeps;
+  return PD_OK;
+}
+
+static bool validPlan(const pd_plan& p) {
+  return p.team_ctas >= 0 && p.team_ctas <= 1024 && (p.big_cluster_ctas == 0 || (p.big_cluster_ctas >= 2 &&
+         p.big_cluster_ctas <= 16)) && std::isfinite(p.latency_scale) && p.latency_scale >= 0.0 &&
+         p.latency_scale <= 1e3;
+}
+
+int pd_sim_set_plan(pd_sim* s, const pd_plan* plan) {
+  if (!s || !plan) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  if (!validPlan(*plan)) return fail(PD_ERR_INVALID_ARGUMENT, "plan field out of range");
+  SavedSim o;
+  if (const int rc = saveSim(s, o)) return rc;
+  if (const int rc = replan(s, *plan, o, s->logCapacity > 0 ? s->logCapacity : 1)) return rc;
+  return restoreCounters(s, o);
+}
+
+int pd_sim_get_plan(pd_sim* s, pd_plan* out) {
+  if (!s || !out) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = effectivePlan(s);
+  return PD_OK;
+}
+
+int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_substep, int32_t* n_tried,
+                    int32_t* chosen) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (substeps <= 0) return fail(PD_ERR_INVALID_ARGUMENT, "substeps must be > 0");
+  SavedSim o;
+  if (const int rc = saveSim(s, o)) return rc;
+  const int capacity = std::max(s->logCapacity, substeps);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PD_CUDA(cudaEventCreate(&e0));
+  PD_CUDA(cudaEventCreate(&e1));
+  std::vector<pd_plan> plans, effective;
+  std::vector<double> times;
+  int rc = PD_OK;
+  auto run = [&](const pd_plan& p) {
+    if (rc != PD_OK || plans.size() >= PD_TUNE_MAX_CANDIDATES) return;
+    double ms = 0.0;
+    rc = replan(s, p, o, capacity);
+    if (rc == PD_OK) rc = timeSubsteps(s, substeps, e0, e1, &ms);
+    if (rc != PD_OK) return;
+    plans.push_back(p);
+    effective.push_back(effectivePlan(s));
+    times.push_back(ms);
+  };
+  auto best = [&]() {
+    size_t b = 0;
+    for (size_t i = 1; i < times.size(); ++i)
+      if (times[i] < times[b]) b = i;
+    return b;
+  };
+  const pd_plan start = s->plan;
+  run(start);  // candidate 0: the plan in force
+  const int p = s->precision();
+  const int count = static_cast<int>(s->inst.size());
+  if (rc == PD_OK && p != PD_PRECISION_FP64_EXACT) {
+    const int team0 = s->teamCtas;
+    const bool delta = s->delta, corr = s->corr, supernodal = !s->delta && !s->dense;
+    if (delta) {  // team sizes below the built-in SMs ÷ cloths
+      for (int t : {team0 * 3 / 4, team0 / 2, team0 / 4})
+        if (t >= 2 && t != team0) {
+          pd_plan c = start;
+          c.team_ctas = t;
+          run(c);
+        }
+    } else if (corr && count > 1 && team0 == 1) {  // a batch: which cloths run as clusters, how large
+      for (int minN : {-1, 4096, 8192, 12288})
+        for (int cs : {2, 4, 8}) {
+          if (minN < 0 && cs != 4) continue;
+          pd_plan c = start;
+          c.big_min_vertices = minN;
+          c.big_cluster_ctas = cs;
+          if (minN == effective[0].big_min_vertices && cs == effective[0].big_cluster_ctas) continue;
+          run(c);
+        }
+    } else {  // CTAs per cloth of the cluster kernels
+      const std::vector<int> sizes = count <= 9 ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{1, 2, 4};
+      for (int t : sizes)
+        if (t != team0) {
+          pd_plan c = start;
+          c.team_ctas = t;
+          run(c);
+        }
+    }
+    if (supernodal) {  // then the lane model's latency weight for the best so far
+      const pd_plan b = plans[best()];
+      for (double w : {0.5, 2.0}) {
+        pd_plan c = b;
+        c.latency_scale = w;
+        run(c);
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != PD_OK) return rc;
+  const size_t b = best();
+  if (const int rc2 = replan(s, plans[b], o, s->logCapacity > 0 ? s->logCapacity : 1)) return rc2;
+  if (const int rc2 = restoreCounters(s, o)) return rc2;
+  const size_t k = std::min<size_t>(plans.size(), PD_TUNE_MAX_CANDIDATES);
+  for (size_t i = 0; i < k; ++i) {
+    if (tried) tried[i] = effective[i];
+    if (ms_per_substep) ms_per_substep[i] = times[i];
+  }
+  if (n_tried) *n_tried = static_cast<int32_t>(k);
+  if (chosen) *chosen = static_cast<int32_t>(b);
   return PD_OK;
 }
 

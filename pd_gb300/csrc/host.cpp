@@ -405,7 +405,7 @@ int phaseLength(const Factor& f, int i, int ph) {
 }
 }  // namespace
 
-std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas) {
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas, double latencyScale) {
   const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
   std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
   for (int l = 0; l < nlev; ++l)
@@ -428,7 +428,7 @@ std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ct
         // trips of the row loop, ~8 cycles per dependent FMA, ~30 per shuffle step
         const double trips = std::ceil(static_cast<double>(lmax) / G);
         const double issue = R * G / 32.0 * (3.0 * std::ceil(lavg / G) + 4.0 * lg + 6.0) / (4.0 * ctas);
-        const double chain = std::ceil(R * G / static_cast<double>(ctaThreads * ctas)) *
+        const double chain = latencyScale * std::ceil(R * G / static_cast<double>(ctaThreads * ctas)) *
                              (600.0 * std::ceil(trips / 4.0) + 8.0 * trips + 30.0 * lg + 600.0);
         const double cost = std::max(issue, chain);
         if (cost < best) {
@@ -466,7 +466,7 @@ void buildMixed(Factor& f, const ScalarMatrix& A) {
   }
 }
 
-std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
+std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas, double latencyScale) {
   const int nlev = static_cast<int>(f.lvlRowPtr.size()) - 1;
   std::vector<int32_t> g(4 * static_cast<size_t>(std::max(nlev, 0)), 1);
   // every CTA of the FP64 kernels runs 256 threads
@@ -501,7 +501,8 @@ std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas) {
         const double total = R * G / 32.0 * perRowInstr * 80.0;
         const double rowsPerGroup = std::ceil(R * G / threads);
         const double trips = std::ceil(static_cast<double>(lmax) / G);
-        const double chain = rowsPerGroup * (700.0 * std::ceil(trips / 4.0) + 64.0 * trips + 100.0 * lg + 700.0);
+        const double chain =
+            latencyScale * rowsPerGroup * (700.0 * std::ceil(trips / 4.0) + 64.0 * trips + 100.0 * lg + 700.0);
         const double cost = std::max(total / smsps, chain);
         if (cost < best) {
           best = cost;

@@ -98,9 +98,11 @@ void buildSupernodal(Factor& f, const SupernodeTree& tree);
 // of 256 threads, from a cost model of FP64 warp instructions: on GB300 an FP64 warp
 // instruction occupies its SMSP's pipe for ~80 cycles whatever its active lanes, so narrow groups
 // waste fewer lanes while wide groups spread a level's few long rows over more SMSPs.
-std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas);
+// latencyScale weights the dependent-latency term against the issue term (1: the model as
+// calibrated; the autotuner tries others).
+std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas, double latencyScale = 1.0);
 // The same for an FP32 solve run by `ctas` CTAs of `ctaThreads` threads, where latency dominates.
-std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas = 1);
+std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas = 1, double latencyScale = 1.0);
 // Fills the mixed-precision fields of a factorized Factor (needs the supernodal fields).
 void buildMixed(Factor& f, const ScalarMatrix& A);
 
