@@ -584,8 +584,8 @@ struct pd_sim {
   std::vector<pdg::HostStateDev> hostTable;   // device-visible addresses; empty unless all are page-locked
   pdg::HostStateDev* dHostTable = nullptr;
   unsigned tableGen = ~0u;
-  int* dNonFinite = nullptr;                  // set by the gather on a non-finite position
-  int* hNonFinite = nullptr;                  // its page-locked copy, read after the step
+  int* hStatus = nullptr;                     // mapped host words: [0] non-finite input, [1] team error
+  int* dStatus = nullptr;                     // their device-visible address
   cudaGraphExec_t graphExec = nullptr;        // gather → substeps → scatter, replayed per call
   int graphSubsteps = -1;
   unsigned graphGen = ~0u;
@@ -598,8 +598,7 @@ struct pd_sim {
     if (joinEv) cudaEventDestroy(joinEv);
     dropGraph();
     if (dHostTable) cudaFree(dHostTable);
-    if (dNonFinite) cudaFree(dNonFinite);
-    if (hNonFinite) cudaFreeHost(hNonFinite);
+    if (hStatus) cudaFreeHost(hStatus);
     if (ownStream) cudaStreamDestroy(ownStream);
   }
   void dropGraph() {
@@ -942,7 +941,7 @@ struct pd_sim {
     return PD_OK;
   }
 
-  // Records gather → substeps → scatter → copy of the non-finite flag on `st` as a CUDA graph.
+  // Records gather → substeps → scatter on `st` as a CUDA graph.
   int captureHostStep(cudaStream_t st, int substeps) {
     dropGraph();
     const int count = static_cast<int>(inst.size());
@@ -950,11 +949,10 @@ struct pd_sim {
     for (const auto& I : inst) maxN = std::max(maxN, I.scene.n);
     PD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = PD_OK;
-    cudaError_t e = cudaMemsetAsync(dNonFinite, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = static_cast<cudaError_t>(pdg::launchGatherState(dHostTable, count, maxN, dNonFinite, st));
+    cudaError_t e = static_cast<cudaError_t>(pdg::launchGatherState(dHostTable, count, maxN, dStatus, st));
     if (e == cudaSuccess && substeps > 0) rc = launchSubsteps(st, substeps);
-    if (e == cudaSuccess && rc == PD_OK) e = static_cast<cudaError_t>(pdg::launchScatterState(dHostTable, count, maxN, st));
-    if (e == cudaSuccess && rc == PD_OK) e = cudaMemcpyAsync(hNonFinite, dNonFinite, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && rc == PD_OK)
+      e = static_cast<cudaError_t>(pdg::launchScatterState(dHostTable, count, maxN, dStatus, st));
     cudaGraph_t g = nullptr;
     const cudaError_t ee = cudaStreamEndCapture(st, &g);
     if (rc == PD_OK && (e != cudaSuccess || ee != cudaSuccess))
@@ -1398,24 +1396,27 @@ int pd_sim_step_host(pd_sim* s, int32_t substeps) {
     for (size_t i = 0; i < count; ++i) {
       s->hostTable[i].dx = reinterpret_cast<double*>(s->dArena + s->inst[i].oX);
       s->hostTable[i].dv = reinterpret_cast<double*>(s->dArena + s->inst[i].oV);
+      s->hostTable[i].err = s->delta ? reinterpret_cast<const int32_t*>(s->dArena + s->inst[i].oErr) : nullptr;
     }
     if (!s->dHostTable) PD_CUDA(cudaMalloc(&s->dHostTable, sizeof(pdg::HostStateDev) * count));
     PD_CUDA(cudaMemcpy(s->dHostTable, s->hostTable.data(), sizeof(pdg::HostStateDev) * count,
                        cudaMemcpyHostToDevice));
     s->tableGen = s->generation;
   }
-  if (!s->dNonFinite) {
-    PD_CUDA(cudaMalloc(&s->dNonFinite, sizeof(int)));
-    PD_CUDA(cudaHostAlloc(&s->hNonFinite, sizeof(int), cudaHostAllocDefault));
+  if (!s->hStatus) {
+    PD_CUDA(cudaHostAlloc(&s->hStatus, 2 * sizeof(int), cudaHostAllocMapped));
+    PD_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->dStatus), s->hStatus, 0));
   }
   if (!s->graphExec || s->graphSubsteps != substeps || s->graphGen != s->generation)
     if (const int rc = s->captureHostStep(st, substeps)) return rc;
-  *s->hNonFinite = 0;
+  volatile int* status = s->hStatus;
+  status[0] = status[1] = 0;
   PD_CUDA(cudaGraphLaunch(s->graphExec, st));
   if (substeps > 0) s->lastSubsteps = substeps;
-  if (st != s->stream) PD_CUDA(cudaStreamSynchronize(st));
-  if (const int rc_ = s->sync()) return rc_;
-  if (*s->hNonFinite)
+  PD_CUDA(cudaStreamSynchronize(st));
+  if (status[1])  // a team exchange gave up: report it and reset the exchange words
+    if (const int rc_ = s->sync()) return rc_;
+  if (status[0])
     return fail(PD_ERR_INVALID_ARGUMENT, "a bound position array holds a non-finite value (the step ran on it)");
   return PD_OK;
 }

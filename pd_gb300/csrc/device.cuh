@@ -207,13 +207,15 @@ struct HostStateDev {
   double* hv;
   double* dx;
   double* dv;
+  const int32_t* err;  // the instance's team-exchange error flag, or null
   int32_t n;
 };
-// Host → arena for every instance (grid: chunks × instances, count ≤ 65535); sets *dNonFinite
-// when a position is not finite. maxN: the largest instance's vertex count.
-int launchGatherState(const HostStateDev* dTable, int count, int maxN, int* dNonFinite, void* stream);
-// Arena → host for every instance.
-int launchScatterState(const HostStateDev* dTable, int count, int maxN, void* stream);
+// Host → arena for every instance (grid: chunks × instances, count ≤ 65535); sets status[0] when
+// a position is not finite. maxN: the largest instance's vertex count. status: two ints in mapped
+// host memory (device-visible address).
+int launchGatherState(const HostStateDev* dTable, int count, int maxN, int* status, void* stream);
+// Arena → host for every instance; sets status[1] when an instance's error flag is set.
+int launchScatterState(const HostStateDev* dTable, int count, int maxN, int* status, void* stream);
 
 constexpr int kBlockThreads = 256;   // one CTA per cloth (several CTAs share an SM in a batch), and
                                       // the CTAs of the FP64 cluster kernel (fewer threads per
