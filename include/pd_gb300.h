@@ -252,6 +252,25 @@ int pd_sim_device_state(pd_sim* s, int32_t instance, double** positions, double*
 int pd_sim_bind_host(pd_sim* s, double* const* positions, double* const* velocities);
 int pd_sim_step_host(pd_sim* s, int32_t substeps);
 
+/* ---- Spectrum of the linearised PD iteration (the reference's _verify/iteration_spectrum.cpp) ----
+ * At instance i's current positions: T = I − A⁻¹(M/h² + N + K_b), N = Σ_e κ_e A_eᵀ(n_e n_eᵀ)A_e with
+ * n_e = unit(x_a − x_b), K_b = Σ_s k·A_sᵀA_s (bending stencils, whose projection is constant; the
+ * reference's tool refuses them), pinned rows zeroed; B = I − T. `power_iterations` steps of power
+ * iteration from the reference's start vector (std::mt19937(12345), (rng() % 2000)/1000 − 1 per
+ * free component in vertex order), on the GPU with the FP64 supernodal solve. Returns the last
+ * ‖y‖/‖x‖ estimates and the ones before them (their gap shows whether the iteration has
+ * settled), λ_min(B) = 1 − ρ(T) and the Chebyshev rate (1 − √(λ_min/λ_max)) / (1 + √(λ_min/λ_max)).
+ * Blocks until done; the state is unchanged. */
+typedef struct pd_spectrum {
+  double rho_plain;        /* ρ(T): predicted contraction per plain PD iteration */
+  double rho_plain_prev;
+  double lambda_max;       /* λ_max(B) */
+  double lambda_max_prev;
+  double lambda_min;       /* 1 − ρ(T) */
+  double rho_cheb;         /* Chebyshev semi-iteration rate over [λ_min, λ_max] */
+} pd_spectrum;
+int pd_sim_spectrum(pd_sim* s, int32_t instance, int32_t power_iterations, pd_spectrum* out);
+
 /* ---- Launch plan and autotuner (the north star's "level-group and tile sizes chosen by an
  * autotuner"; no counterpart in the reference, whose solve runs on host threads) ----
  * A plan overrides the planner's built-in choices; 0 keeps the built-in choice of a field. */

@@ -110,6 +110,8 @@ def lib():
     L.oracle_project_one.argtypes = [dp, dp, C.c_double, dp]
     L.oracle_sim_gradient.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp]
     L.oracle_sim_gradient.restype = C.c_int
+    L.oracle_sim_spectrum.argtypes = [C.c_void_p, C.c_int, dp]
+    L.oracle_sim_spectrum.restype = C.c_int
     _lib = L
     return L
 
@@ -358,6 +360,14 @@ class OracleSim:
         if rc != 0:
             raise RuntimeError("oracle gradient failed")
         return dict(loss=loss.value, dkappa=dk, dv0=dv, dforce=df)
+
+    def spectrum(self, iters=400):
+        """Power-iteration estimates at the current positions: rho_plain (ρ(T)) and lambda_max
+        (λ_max(B)) with the estimates one iteration earlier (iteration_spectrum.cpp)."""
+        out = np.zeros(4)
+        if self._L.oracle_sim_spectrum(self._h, int(iters), _ptr(out, C.c_double)) != 0:
+            raise RuntimeError("factorization failed")
+        return dict(rho_plain=out[0], rho_plain_prev=out[1], lambda_max=out[2], lambda_max_prev=out[3])
 
     def rhs(self, base, overwrite_pins=True):
         base = np.ascontiguousarray(base, np.float64).reshape(-1)

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <random>
 #include <set>
 #include <vector>
 
@@ -1274,6 +1275,92 @@ extern "C" int oracle_sim_solve(oracle_sim* s, const double* b, double* x) {
   if (!s->factorReady) return -1;
   std::vector<double> w(s->n);
   for (int c = 0; c < 3; ++c) solveComponent(*s, c, b, x, w.data());
+  return 0;
+}
+
+// Spectrum of the linearised PD iteration (_verify/iteration_spectrum.cpp:126-338) at the current
+// positions: T = I − A⁻¹(M/h² + N), N = Σ_e κ_e A_eᵀ(n_e n_eᵀ)A_e with n_e = unit(x_a − x_b)
+// (:133-142, :229-263), pinned rows of the right-hand side zeroed (:255-262). Power iteration from
+// the reference's start vector — std::mt19937(12345), (rng() % 2000)/1000 − 1 on every free
+// component in vertex order (:319-324) — recording ‖y‖/‖x‖ for the last 20 iterations (:282-306):
+// out[0] = ρ(T) (last estimate), out[1] = the one before, out[2] = λ_max(B) for B = I − T from the
+// same start, out[3] = the one before. Bending stencils (which the reference's tool refuses, :113-116)
+// enter as their full term k·A_sᵀA_s: their projection is constant, so B gains that block of A.
+extern "C" int oracle_sim_spectrum(oracle_sim* s, int iters, double* out) {
+  if (!s->factorReady) oracle_sim_factor(s, nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (!s->factorReady) return -1;
+  const int n = s->n, dim = 3 * n;
+  const double invH2 = 1.0 / (s->cfg.dt * s->cfg.dt);
+  std::vector<V3> nE(s->edges.size());
+  for (size_t c = 0; c < s->edges.size(); ++c) {
+    const Edge& e = s->edges[c];
+    const V3 rel = sub(ld(&s->x[3 * static_cast<size_t>(e.a)]), ld(&s->x[3 * static_cast<size_t>(e.b)]));
+    const double len = length(rel);
+    nE[c] = (len > 0.0) ? mul(rel, 1.0 / len) : V3{0, 0, 0};
+  }
+  std::vector<double> rhs(dim), sol(dim), w(n);
+  auto applyInertiaPlusN = [&](const std::vector<double>& x) {
+    std::fill(rhs.begin(), rhs.end(), 0.0);
+    for (int v = 0; v < n; ++v) {
+      if (s->pinned[v]) continue;
+      const double d = s->m[v] * invH2;
+      for (int c = 0; c < 3; ++c) rhs[3 * v + c] = d * x[3 * v + c];
+    }
+    for (size_t c = 0; c < s->edges.size(); ++c) {
+      const Edge& e = s->edges[c];
+      const V3& g = nE[c];
+      if (e.k == 0.0 || (g.x == 0.0 && g.y == 0.0 && g.z == 0.0)) continue;
+      const V3 rel{x[3 * e.a] - x[3 * e.b], x[3 * e.a + 1] - x[3 * e.b + 1], x[3 * e.a + 2] - x[3 * e.b + 2]};
+      const double dot = g.x * rel.x + g.y * rel.y + g.z * rel.z;
+      const V3 sc = mul(g, e.k * dot);
+      rhs[3 * e.a] += sc.x;
+      rhs[3 * e.a + 1] += sc.y;
+      rhs[3 * e.a + 2] += sc.z;
+      rhs[3 * e.b] -= sc.x;
+      rhs[3 * e.b + 1] -= sc.y;
+      rhs[3 * e.b + 2] -= sc.z;
+    }
+    for (int v = 0; v < n; ++v) {  // k·A_sᵀA_s of the stencils at v, in stencil order
+      if (s->pinned[v] || s->bstencils.empty()) continue;
+      for (uint32_t k = s->bstart[v]; k < s->bstart[v + 1]; ++k) {
+        const Bend& b = s->bends[s->bstencils[k]];
+        const double fac = -b.k * s->bweight[k];
+        for (int c = 0; c < 3; ++c)
+          rhs[3 * v + c] -= fac * (x[3 * b.a + c] - 2.0 * x[3 * b.b + c] + x[3 * b.c + c]);
+      }
+    }
+    for (int v = 0; v < n; ++v)
+      if (s->pinned[v]) rhs[3 * v] = rhs[3 * v + 1] = rhs[3 * v + 2] = 0.0;
+  };
+  auto norm = [](const std::vector<double>& a) {
+    double acc = 0.0;
+    for (double t : a) acc += t * t;
+    return std::sqrt(acc);
+  };
+  auto power = [&](bool plain, std::vector<double> x, double* last, double* prev) {
+    std::vector<double> y(dim);
+    *last = *prev = 0.0;
+    for (int it = 0; it < iters; ++it) {
+      applyInertiaPlusN(x);
+      for (int c = 0; c < 3; ++c) solveComponent(*s, c, rhs.data(), sol.data(), w.data());
+      for (int i = 0; i < dim; ++i) y[i] = plain ? x[i] - sol[i] : sol[i];
+      const double ny = norm(y);
+      if (ny <= 0.0) break;
+      if (it >= iters - 20) {
+        *prev = *last;
+        *last = ny / norm(x);
+      }
+      for (int i = 0; i < dim; ++i) x[i] = y[i] / ny;
+    }
+  };
+  std::vector<double> x0(dim, 0.0);
+  std::mt19937 rng(12345);
+  for (int v = 0; v < n; ++v) {
+    if (s->pinned[v]) continue;
+    for (int d = 0; d < 3; ++d) x0[3 * v + d] = static_cast<double>(rng() % 2000) / 1000.0 - 1.0;
+  }
+  power(true, x0, &out[0], &out[1]);
+  power(false, x0, &out[2], &out[3]);
   return 0;
 }
 

@@ -158,6 +158,11 @@ void oracle_sim_bend_rhs(oracle_sim* s, double* out);
 int oracle_sim_gradient(oracle_sim* s, int substeps, const double* targets, const double* force,
                         double* loss, double* dkappa, double* dv0, double* dforce);
 
+/* Power iteration on the linearised PD map at the current positions (the reference's
+ * _verify/iteration_spectrum.cpp): out[0], out[1] = the last two estimates of ρ(T),
+ * T = I − A⁻¹(M/h² + N + Σ_s k·A_sᵀA_s); out[2], out[3] = those of λ_max(B), B = I − T. */
+int oracle_sim_spectrum(oracle_sim* s, int iters, double* out);
+
 /* Closed-form projection of one edge (DistanceTerm::projectOne). */
 void oracle_project_one(const double* pa, const double* pb, double rest, double* out);
 

@@ -91,6 +91,11 @@ class _Plan(C.Structure):
 PD_TUNE_MAX_CANDIDATES = 32
 
 
+class _Spectrum(C.Structure):
+    _fields_ = [("rho_plain", C.c_double), ("rho_plain_prev", C.c_double), ("lambda_max", C.c_double),
+                ("lambda_max_prev", C.c_double), ("lambda_min", C.c_double), ("rho_cheb", C.c_double)]
+
+
 class _SimStats(C.Structure):
     _fields_ = [("iterations_used", C.c_int32), ("converged", C.c_int32),
                 ("early_exit_count", C.c_int32), ("last_residual", C.c_double)]
@@ -136,6 +141,7 @@ _SIGS = {
     "pd_sim_set_state": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
     "pd_sim_device_state": ([C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)], C.c_int),
     "pd_sim_bind_host": ([C.c_void_p, C.POINTER(_dp), C.POINTER(_dp)], C.c_int),
+    "pd_sim_spectrum": ([C.c_void_p, C.c_int32, C.c_int32, C.POINTER(_Spectrum)], C.c_int),
     "pd_sim_autotune": ([C.c_void_p, C.c_int32, C.POINTER(_Plan), _dp, _ip, _ip], C.c_int),
     "pd_sim_set_plan": ([C.c_void_p, C.POINTER(_Plan)], C.c_int),
     "pd_sim_get_plan": ([C.c_void_p, C.POINTER(_Plan)], C.c_int),
@@ -442,6 +448,13 @@ class Simulator:
         _check(self._lib.pd_sim_step_host(self._h, int(substeps)))
         if substeps > 0:
             self._last = int(substeps)
+
+    def spectrum(self, i: int = 0, iters: int = 400) -> dict:
+        """Power-iteration spectrum of the linearised PD map of instance i at its current positions
+        (pd_sim_spectrum; the reference's _verify/iteration_spectrum.cpp)."""
+        out = _Spectrum()
+        _check(self._lib.pd_sim_spectrum(self._h, i, int(iters), C.byref(out)))
+        return {f: getattr(out, f) for f, _ in _Spectrum._fields_}
 
     def autotune(self, substeps: int = 10) -> dict:
         """Times candidate launch plans on this batch and keeps the fastest (pd_sim_autotune); the

@@ -29,6 +29,7 @@ UNITS = {
     "adjoint.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],
     "state_copy.cu": [],
+    "spectrum.cu": ["-fmad=false"],
 }
 
 

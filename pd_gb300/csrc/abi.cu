@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -1556,6 +1557,47 @@ int pd_sim_get_stats(pd_sim* s, int32_t i, pd_sim_stats* out) {
   out->iterations_used = ints[0];
   out->converged = ints[1];
   out->early_exit_count = ints[2];
+  return PD_OK;
+}
+
+// ------------------------------------------------------------------------------ spectrum
+int pd_sim_spectrum(pd_sim* s, int32_t i, int32_t iters, pd_spectrum* out) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
+  if (iters < 1 || iters > (1 << 20)) return fail(PD_ERR_INVALID_ARGUMENT, "power_iterations must be in [1, 2^20]");
+  if (const int rc_ = s->sync()) return rc_;
+  const Instance& I = s->inst[i];
+  const size_t n3 = 3 * static_cast<size_t>(I.scene.n), e3 = 3 * std::max<size_t>(1, I.scene.edges.size());
+  std::vector<double> x0(n3, 0.0);  // iteration_spectrum.cpp:319-324
+  std::mt19937 rng(12345);
+  for (int v = 0; v < I.scene.n; ++v) {
+    if (I.scene.pinned[v]) continue;
+    for (int d = 0; d < 3; ++d) x0[3 * v + d] = static_cast<double>(rng() % 2000) / 1000.0 - 1.0;
+  }
+  double* work = nullptr;
+  PD_CUDA(cudaMalloc(&work, sizeof(double) * (3 * n3 + e3 + 4)));
+  double* dx0 = work;
+  double* dp = work + n3;
+  double* dy = work + 2 * n3;
+  double* dnE = work + 3 * n3;
+  double* dout = dnE + e3;
+  double res[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(dx0, x0.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s->stream);
+  const int cs = I.scene.n >= 1024 ? 16 : I.scene.n >= 256 ? 4 : 1;
+  if (e == cudaSuccess)
+    e = static_cast<cudaError_t>(pdg::launchSpectrum(s->dDesc + i, dx0, dp, dy, dnE, dout, iters, cs, s->stream));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(res, dout, sizeof(res), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(work);
+  if (e != cudaSuccess) return cudaFail(e, "spectrum");
+  out->rho_plain = res[0];
+  out->rho_plain_prev = res[1];
+  out->lambda_max = res[2];
+  out->lambda_max_prev = res[3];
+  out->lambda_min = 1.0 - res[0];
+  const double sq = std::sqrt(out->lambda_min / out->lambda_max);
+  out->rho_cheb = (1.0 - sq) / (1.0 + sq);
   return PD_OK;
 }
 

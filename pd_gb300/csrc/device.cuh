@@ -200,6 +200,12 @@ int gradClusterSupported(int clusterSize);
 // columns per CTA, one in each component of the solve.
 int launchDenseInverse(const InstanceDev* dInstance, int n, void* stream);
 
+// Power iteration on the linearised PD map of one instance at its positions (spectrum.cu):
+// out[0..3] = ρ(T), its previous estimate, λ_max(B), its previous estimate. Work arrays of 3n
+// (x0, p, y) and 3E (nE) doubles; a cluster of clusterSize CTAs when the device runs it, else one.
+int launchSpectrum(const InstanceDev* dInstance, const double* x0, double* p, double* y, double* nE, double* out,
+                   int iters, int clusterSize, void* stream);
+
 // One instance's state in the caller's page-locked host arrays (device-visible addresses) and in
 // the arena (state_copy.cu).
 struct HostStateDev {

@@ -395,3 +395,62 @@ def test_residual_trace_matches_gate(oracle):
     assert np.array_equal((~np.isnan(tr)).sum(axis=1), it) and (it < 30).any()
     last = tr[-1][~np.isnan(tr[-1])][-1]
     assert last == a.stats()["last_residual"] == b.stats()["last_residual"]
+
+
+# ------------------------------------------- spectrum of the PD map (_verify/iteration_spectrum.cpp)
+def test_spectrum_spring_closed_form(oracle):
+    """One free vertex on one edge to a pinned vertex: B = (m/h²·I + κ·n nᵀ)/(m/h² + κ), so
+    λ_max(B) = 1 (along the edge) and ρ(T) = κ/(m/h² + κ) (across it)."""
+    s = spring(oracle, 0.12)
+    r = s.spectrum(60)
+    mh2 = M / (H * H)
+    assert abs(r["rho_plain"] - K / (mh2 + K)) <= 1e-14
+    assert abs(r["lambda_max"] - 1.0) <= 1e-14
+
+
+def _dense_pd_operator(oracle, s, mesh):
+    """B = A⁻¹(M/h² + N + Σ_s k·A_sᵀA_s) on the free components, built densely from the oracle's
+    assembled A and the current positions."""
+    n = mesh.positions.shape[0]
+    rp, ci, val = s.matrix()
+    A = np.zeros((n, n))
+    for r in range(n):
+        A[r, ci[rp[r]:rp[r + 1]]] = val[rp[r]:rp[r + 1]]
+    A3 = np.kron(A, np.eye(3))
+    x, _ = s.state()
+    C = np.zeros((3 * n, 3 * n))
+    h = s.cfg.dt if hasattr(s, "cfg") else H
+    for v in range(n):
+        C[3 * v:3 * v + 3, 3 * v:3 * v + 3] += mesh.masses[v] / (h * h) * np.eye(3)
+    for (a, b), k in zip(mesh.edges, mesh.edge_k):
+        rel = x[a] - x[b]
+        nn = rel / np.linalg.norm(rel)
+        P = k * np.outer(nn, nn)
+        for i, j, sg in ((a, a, 1), (b, b, 1), (a, b, -1), (b, a, -1)):
+            C[3 * i:3 * i + 3, 3 * j:3 * j + 3] += sg * P
+    w = (1.0, -2.0, 1.0)
+    for (a, b, c), k in zip(mesh.bends, mesh.bend_k):
+        vs = (a, b, c)
+        for p in range(3):
+            for q in range(3):
+                C[3 * vs[p]:3 * vs[p] + 3, 3 * vs[q]:3 * vs[q] + 3] += k * w[p] * w[q] * np.eye(3)
+    free = np.repeat(mesh.pinned == 0, 3)
+    Bm = np.linalg.solve(A3, C)
+    return Bm[np.ix_(free, free)]
+
+
+def test_spectrum_matches_dense_eigenvalues(oracle):
+    """A 6×5 cloth with shear and bending, moved off its rest pose: the power-iteration estimates
+    against the eigenvalues of the dense operator."""
+    spec = oracle.GridSpec(nx=6, ny=5, spacing=0.1, stiffness=3000.0, shear_stiffness=900.0, bend_stiffness=40.0)
+    mesh = oracle.make_grid(spec)
+    cfg = oracle.Config(dt=1.0 / 120.0, max_iterations=20, residual_tolerance=0.0, rel_tolerance=0.0,
+                        abs_tolerance=0.0)
+    s = oracle.OracleSim(mesh, cfg)
+    s.step(15)
+    ev = np.linalg.eigvals(_dense_pd_operator(oracle, s, mesh)).real
+    r = s.spectrum(4000)
+    assert abs(r["lambda_max"] - ev.max()) <= 1e-9
+    # T's two largest |eigenvalues| nearly coincide here, so the estimate settles more slowly
+    assert abs(r["rho_plain"] - np.max(np.abs(1.0 - ev))) <= 1e-6
+    assert 0.0 < ev.min() and ev.max() <= 1.0 + 1e-12  # B's spectrum lies in (0, 1]
