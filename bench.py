@@ -77,6 +77,7 @@ def parse():
     p.add_argument("--no-fp64-gpu", action="store_true")
     p.add_argument("--no-cheb", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--no-refactor", action="store_true")
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--grad-side", type=int, default=64)         # smaller only for profiling captures
@@ -365,6 +366,27 @@ def time_fp64_one_at_a_time(P, args, budget_s=120.0):
             "how": "one cloth per launch, plain FP64 path, per-cloth launch times summed"}
 
 
+def refactor_times(P, scenes, cfgs):
+    """A stiffness change of cloth 0 (every κ × 1.1, then × 1.2): milliseconds of the numeric
+    refactorization on the GPU (the default outside FP64_EXACT) and through the host LDLᵀ
+    (PD_GB300_HOST_REFACTOR=1), each including the re-upload and, for the team kernel, the
+    explicit inverse."""
+    sim = P.Simulator([scenes[0]], [cfgs[0]])
+    k = np.asarray(scenes[0].edge_stiffness, np.float64)
+    out = {}
+    for name, scale, host in (("device_ms", 1.1, False), ("host_ms", 1.2, True)):
+        if host:
+            os.environ["PD_GB300_HOST_REFACTOR"] = "1"
+        try:
+            t0 = time.perf_counter()
+            sim.set_edge_stiffness(k * scale)
+            out[name] = (time.perf_counter() - t0) * 1e3
+        finally:
+            os.environ.pop("PD_GB300_HOST_REFACTOR", None)
+    out["device_factorizations"] = sim.info(0)["device_factorize_count"]
+    return out
+
+
 def position_error(P, args, scenes, cfgs, substeps, plan=None):
     """max |x_gpu − x_oracle| / max |x_oracle| after `substeps` substeps from the initial state, this
     precision mode against the FP64 CPU oracle, for the run as timed: every cloth on one handle with
@@ -476,8 +498,10 @@ def run_ours(args):
 
     # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
     # error of this mode against the FP64 CPU oracle after the workload's full substep count
-    fp64_line = pos_err = None
+    fp64_line = pos_err = refactor = None
     if rank == 0:
+        if len(scenes) == 1 and not args.no_refactor:
+            refactor = refactor_times(P, scenes, cfgs)
         if not args.no_fp64_gpu:
             fp64_line = (time_fp64_one_at_a_time(P, args) if len(scenes) > 1
                          else time_fp64_gpu(P, args, stream, flush))
@@ -508,7 +532,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "pd_sim_step_host (gather kernel, substep, scatter kernel: one CUDA graph)"
                         if info["host_state"] == P.PD_HOST_STATE_GRAPH else "pd_sim_step_host (cudaMemcpyAsync per array)"},
-                "clocks": clocks, "plan": plan, "autotune": tune}
+                "clocks": clocks, "plan": plan, "autotune": tune, "refactor": refactor}
         if PRECISIONS[args.precision][0] <= 1:
             ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
             fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU

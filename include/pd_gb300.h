@@ -193,6 +193,8 @@ typedef struct pd_sim_info {
   int32_t cluster_ctas;          /* CTAs running each cloth */
   int32_t solve_kind;            /* PD_SOLVE_* */
   int32_t host_state;            /* PD_HOST_STATE_*: how pd_sim_step_host moves the bound arrays */
+  int32_t device_factorize_count; /* of factorize_count: numeric refactorizations run on the GPU
+                                     (same pattern, new values; every mode but FP64_EXACT) */
 } pd_sim_info;
 
 #define PD_HOST_STATE_NONE 0     /* no host arrays bound */

@@ -80,6 +80,7 @@ class _SimInfo(C.Structure):
         ("forward_levels", C.c_int32), ("backward_levels", C.c_int32),
         ("factorize_count", C.c_int32), ("analyze_count", C.c_int32), ("device_bytes", C.c_int64),
         ("cluster_ctas", C.c_int32), ("solve_kind", C.c_int32), ("host_state", C.c_int32),
+        ("device_factorize_count", C.c_int32),
     ]
 
 

@@ -30,6 +30,7 @@ UNITS = {
     "solve_noalloc.cu": ["-fmad=false"],
     "state_copy.cu": [],
     "spectrum.cu": ["-fmad=false"],
+    "refactor.cu": ["-fmad=false"],
 }
 
 

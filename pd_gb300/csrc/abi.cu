@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <random>
 #include <string>
 #include <vector>
@@ -96,7 +97,10 @@ struct Instance {
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
       oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
       oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl, oXhl,
-      oXhatHl;
+      oXhatHl, oD, oCscToCsr, oAPosCsc, oAPosDiag, oSnByLevel;
+  bool gpuRefactor = false;   // the next upload computes the factor's values on the device
+  int deviceRefactorCount = 0;
+  std::vector<int32_t> patRowptr, patCol;  // pattern of Ã the current symbolic factor was built for
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
   int corrTeam = 1;     // correction kernel: CTAs (a cluster when > 1) running this instance
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
@@ -114,6 +118,14 @@ bool projection32(int p) { return p == PD_PRECISION_FP32_PROJECTION || p == PD_P
 // bytes of per-CTA workspace: reference order w; supernodal w, t; mixed B, X0 (FP64) and Y, T (FP32)
 int workspaceBytesPerVertex(int p) { return mixedSolve(p) ? 72 : (p == PD_PRECISION_FP64_EXACT ? 24 : 48); }
 
+// The reference-order mode keeps the host factorization: its bits are part of the parity bar.
+// PD_GB300_HOST_REFACTOR=1 forces the host path for every mode (to compare the two).
+bool deviceRefactorAllowed(int precision) {
+  if (precision == PD_PRECISION_FP64_EXACT) return false;
+  const char* env = std::getenv("PD_GB300_HOST_REFACTOR");
+  return !(env && env[0] == '1');
+}
+
 std::string prepare(Instance& I, bool reanalyze) {
   const auto& c = I.cfg;
   if (!(c.dt > 0.0)) return "dt must be positive";
@@ -130,9 +142,22 @@ std::string prepare(Instance& I, bool reanalyze) {
   } else {
     perm = I.F.perm;
   }
-  if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
-  pdg::buildSupernodal(I.F, I.tree);
-  pdg::buildMixed(I.F, I.L);
+  if (!reanalyze && !perm.empty() && deviceRefactorAllowed(c.precision) && I.F.maxRowLen > 0 &&
+      I.L.rowptr == I.patRowptr && I.L.col == I.patCol &&
+      pdg::refactorSmemBytes(I.F.maxRowLen) <= 200 * 1024) {
+    // same pattern, new values: the numeric LDLᵀ runs on the device at the next upload
+    pdg::refreshAval(I.F, I.L);
+    I.gpuRefactor = true;
+  } else {
+    if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
+    pdg::buildSupernodal(I.F, I.tree);
+    pdg::buildMixed(I.F, I.L);
+    if (c.precision != PD_PRECISION_FP64_EXACT) pdg::buildRefactorMaps(I.F);
+    else I.F.maxRowLen = 0;
+    I.patRowptr = I.L.rowptr;
+    I.patCol = I.L.col;
+    I.gpuRefactor = false;
+  }
   I.factorizeCount += 1;
   pdg::assembleBendingRhs(I.scene, I.bendRhs);
   I.stamp = pdg::computeStamp(I.scene, c.dt);
@@ -379,6 +404,11 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencySc
   I.oX0 = A.zeros(24 * n);
   I.oY32 = A.zeros(12 * n);
   I.oT32 = A.zeros(12 * n);
+  I.oD = A.add(I.F.d);
+  I.oCscToCsr = A.add(I.F.cscToCsr);
+  I.oAPosCsc = A.add(I.F.aPosCsc);
+  I.oAPosDiag = A.add(I.F.aPosDiag);
+  I.oSnByLevel = A.add(I.F.snByLevel);
   I.bytes = A.host.size() - before;
 }
 
@@ -764,12 +794,79 @@ struct pd_sim {
     PD_CUDA(cudaMemcpy(dArena, A.host.data(), A.host.size(), cudaMemcpyHostToDevice));
     const int rc = ensureLogs(capacity);
     if (rc != PD_OK) return rc;
+    for (auto& I : inst)  // numeric refactorizations on the device, before anything reads the factor
+      if (I.gpuRefactor)
+        if (const int rc2 = refactorOnDevice(I)) return rc2;
     for (size_t i = 0; i < inst.size(); ++i) {  // explicit inverses from the uploaded FP64 factors
       if (inst[i].denseLd <= 0) continue;
       const int e = pdg::launchDenseInverse(dDesc + i, inst[i].scene.n, stream);
       if (e != 0) return cudaFail(static_cast<cudaError_t>(e), "explicit inverse launch");
     }
     PD_CUDA(cudaStreamSynchronize(stream));  // complete before a later stream change can race it
+    return PD_OK;
+  }
+
+  // LDLᵀ values, block inverses and FP32 copies of instance I computed on the device from the
+  // uploaded Ã (refactor.cu), then copied back into the host factor, which stays the reference
+  // for later uploads and for pd_sim_get_factor.
+  int refactorOnDevice(Instance& I) {
+    pdg::Factor& F = I.F;
+    auto P = [&](size_t off) { return dArena + off; };
+    int* dStatus = nullptr;
+    PD_CUDA(cudaMalloc(&dStatus, sizeof(int)));
+    pdg::RefactorDev r{};
+    r.n = F.n;
+    r.maxRowLen = F.maxRowLen;
+    r.nnz = static_cast<int64_t>(F.colval.size());
+    r.nInv = static_cast<int64_t>(F.invL.size());
+    r.colptr = reinterpret_cast<const int32_t*>(P(I.oLcp));
+    r.rowidx = reinterpret_cast<const int32_t*>(P(I.oLri));
+    r.colval = reinterpret_cast<double*>(P(I.oLcv));
+    r.rowptr = reinterpret_cast<const int32_t*>(P(I.oLrp));
+    r.colidx = reinterpret_cast<const int32_t*>(P(I.oLci));
+    r.rowval = reinterpret_cast<double*>(P(I.oLrv));
+    r.d = reinterpret_cast<double*>(P(I.oD));
+    r.dinv = reinterpret_cast<double*>(P(I.oDinv));
+    r.cscToCsr = reinterpret_cast<const int32_t*>(P(I.oCscToCsr));
+    r.aPosCsc = reinterpret_cast<const int32_t*>(P(I.oAPosCsc));
+    r.aPosDiag = reinterpret_cast<const int32_t*>(P(I.oAPosDiag));
+    r.Aval = reinterpret_cast<const double*>(P(I.oAval));
+    r.snStart = reinterpret_cast<const int32_t*>(P(I.oSnStart));
+    r.offEnd = reinterpret_cast<const int32_t*>(P(I.oOffEnd));
+    r.snInvOff = reinterpret_cast<const int64_t*>(P(I.oSnInv));
+    r.invL = reinterpret_cast<double*>(P(I.oInvL));
+    r.invLT = reinterpret_cast<double*>(P(I.oInvLT));
+    r.rowval32 = reinterpret_cast<float*>(P(I.oLrv32));
+    r.colval32 = reinterpret_cast<float*>(P(I.oLcv32));
+    r.invL32 = reinterpret_cast<float*>(P(I.oInvL32));
+    r.invLT32 = reinterpret_cast<float*>(P(I.oInvLT32));
+    r.dinv32 = reinterpret_cast<float*>(P(I.oDinv32));
+    r.status = dStatus;
+    int status = 0;
+    cudaError_t e = cudaMemsetAsync(dStatus, 0, sizeof(int), stream);
+    const int levels = static_cast<int>(F.snLevelPtr.size()) - 1;
+    const int ns = static_cast<int>(F.snStart.size()) - 1;
+    if (e == cudaSuccess)
+      e = static_cast<cudaError_t>(pdg::launchRefactor(r, reinterpret_cast<const int32_t*>(P(I.oSnByLevel)),
+                                                       F.snLevelPtr.data(), levels, ns, stream));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&status, dStatus, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    cudaFree(dStatus);
+    if (e != cudaSuccess) return cudaFail(e, "device refactorization");
+    if (status != 0)
+      return fail(PD_ERR_FACTORIZATION, "LDL^T pivot " + std::to_string(status - 1) +
+                                            " is zero or not finite: L is not positive definite");
+    auto back = [&](auto& v, size_t off) {
+      using T = typename std::decay_t<decltype(v)>::value_type;
+      return cudaMemcpy(v.data(), P(off), v.size() * sizeof(T), cudaMemcpyDeviceToHost);
+    };
+    for (cudaError_t ee : {back(F.rowval, I.oLrv), back(F.colval, I.oLcv), back(F.d, I.oD), back(F.dinv, I.oDinv),
+                           back(F.invL, I.oInvL), back(F.invLT, I.oInvLT), back(F.rowval32, I.oLrv32),
+                           back(F.colval32, I.oLcv32), back(F.invL32, I.oInvL32), back(F.invLT32, I.oInvLT32),
+                           back(F.dinv32, I.oDinv32)})
+      if (ee != cudaSuccess) return cudaFail(ee, "copy of the device factor");
+    I.gpuRefactor = false;
+    I.deviceRefactorCount += 1;
     return PD_OK;
   }
 
@@ -1538,6 +1635,7 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
   out->analyze_count = I.analyzeCount;
   out->device_bytes = static_cast<int64_t>(I.bytes);
   out->cluster_ctas = (s->corr && I.corrTeam > 1) ? I.corrTeam : s->teamCtas;
+  out->device_factorize_count = I.deviceRefactorCount;
   out->host_state = s->hostX.empty() ? PD_HOST_STATE_NONE : s->hostTable.empty() ? PD_HOST_STATE_COPIES
                                                                                  : PD_HOST_STATE_GRAPH;
   const int p = s->precision();
@@ -2004,6 +2102,7 @@ int pd_scene_factor(const pd_mesh* mesh, const pd_scene_config* cfg, int32_t* pe
     layout(I, A, 1, 0);
     info->cluster_ctas = 1;
     info->host_state = PD_HOST_STATE_NONE;
+    info->device_factorize_count = 0;
     info->solve_kind = I.cfg.precision == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
                        : mixedSolve(I.cfg.precision)              ? PD_SOLVE_SUPERNODAL32
                                                                   : PD_SOLVE_SUPERNODAL;

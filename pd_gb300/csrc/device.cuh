@@ -206,6 +206,43 @@ int launchDenseInverse(const InstanceDev* dInstance, int n, void* stream);
 int launchSpectrum(const InstanceDev* dInstance, const double* x0, double* p, double* y, double* nE, double* out,
                    int iters, int clusterSize, void* stream);
 
+// Device arrays of one instance's factor for the numeric refactorization (refactor.cu).
+struct RefactorDev {
+  int32_t n;
+  int32_t maxRowLen;       // longest CSR row of L
+  int64_t nnz;             // strictly lower entries
+  int64_t nInv;            // entries of the packed block inverses
+  const int32_t* colptr;
+  const int32_t* rowidx;
+  double* colval;
+  const int32_t* rowptr;
+  const int32_t* colidx;
+  double* rowval;
+  double* d;
+  double* dinv;
+  const int32_t* cscToCsr;
+  const int32_t* aPosCsc;
+  const int32_t* aPosDiag;
+  const double* Aval;      // Ã in elimination order (CSR)
+  const int32_t* snStart;
+  const int32_t* offEnd;
+  const int64_t* snInvOff;
+  double* invL;
+  double* invLT;
+  float* rowval32;
+  float* colval32;
+  float* invL32;
+  float* invLT32;
+  float* dinv32;
+  int* status;             // set to j + 1 for a zero or non-finite pivot d_j
+};
+// Shared memory of one level launch for rows of up to maxRowLen entries.
+int refactorSmemBytes(int maxRowLen);
+// LDLᵀ values level by level (supernodes dSnByLevel[snLevelPtr[l] .. snLevelPtr[l+1]) per launch;
+// snLevelPtr is a host array), then the block inverses of the ns supernodes and the FP32 copies.
+int launchRefactor(const RefactorDev& r, const int32_t* dSnByLevel, const int32_t* snLevelPtr, int levels, int ns,
+                   void* stream);
+
 // One instance's state in the caller's page-locked host arrays (device-visible addresses) and in
 // the arena (state_copy.cu).
 struct HostStateDev {

@@ -441,6 +441,49 @@ std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ct
   return g;
 }
 
+void buildRefactorMaps(Factor& f) {
+  const int n = f.n;
+  const int64_t nnz = f.colptr[n];
+  f.cscToCsr.assign(nnz, 0);
+  std::vector<int32_t> cur(f.rowptr.begin(), f.rowptr.end() - 1);
+  for (int c = 0; c < n; ++c)  // the CSR was filled column by column: same walk
+    for (int p = f.colptr[c]; p < f.colptr[c + 1]; ++p) f.cscToCsr[p] = cur[f.rowidx[p]]++;
+  auto find = [&](int row, int col) {
+    const int32_t* b = f.Acol.data() + f.Aptr[row];
+    const int32_t* e = f.Acol.data() + f.Aptr[row + 1];
+    const int32_t* it = std::lower_bound(b, e, col);
+    return (it != e && *it == col) ? static_cast<int32_t>(it - f.Acol.data()) : -1;
+  };
+  f.aPosCsc.assign(nnz, -1);
+  for (int c = 0; c < n; ++c)
+    for (int p = f.colptr[c]; p < f.colptr[c + 1]; ++p) f.aPosCsc[p] = find(f.rowidx[p], c);
+  f.aPosDiag.assign(n, -1);
+  for (int j = 0; j < n; ++j) f.aPosDiag[j] = find(j, j);
+  const int ns = static_cast<int>(f.snLevel.size());
+  int nlev = 0;
+  for (int s = 0; s < ns; ++s) nlev = std::max(nlev, f.snLevel[s] + 1);
+  f.snLevelPtr.assign(nlev + 1, 0);
+  for (int s = 0; s < ns; ++s) f.snLevelPtr[f.snLevel[s] + 1] += 1;
+  for (int l = 0; l < nlev; ++l) f.snLevelPtr[l + 1] += f.snLevelPtr[l];
+  f.snByLevel.assign(ns, 0);
+  std::vector<int32_t> at(f.snLevelPtr.begin(), f.snLevelPtr.end() - 1);
+  for (int s = 0; s < ns; ++s) f.snByLevel[at[f.snLevel[s]]++] = s;
+  f.maxRowLen = 0;
+  for (int r = 0; r < n; ++r) f.maxRowLen = std::max(f.maxRowLen, f.rowptr[r + 1] - f.rowptr[r]);
+}
+
+void refreshAval(Factor& f, const ScalarMatrix& A) {
+  const int n = f.n;
+  std::vector<std::pair<int32_t, double>> row;
+  for (int i = 0; i < n; ++i) {
+    const int v = f.perm[i];
+    row.clear();
+    for (int p = A.rowptr[v]; p < A.rowptr[v + 1]; ++p) row.push_back({f.iperm[A.col[p]], A.val[p]});
+    std::sort(row.begin(), row.end(), [](auto& a, auto& b) { return a.first < b.first; });
+    for (size_t t = 0; t < row.size(); ++t) f.Aval[f.Aptr[i] + t] = row[t].second;
+  }
+}
+
 void buildMixed(Factor& f, const ScalarMatrix& A) {
   auto toF = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
   f.rowval32 = toF(f.rowval);

@@ -77,6 +77,12 @@ struct Factor {
   std::vector<float> rowval32, colval32, invL32, invLT32, dinv32;
   std::vector<int32_t> Aptr, Acol;
   std::vector<double> Aval;
+
+  // Numeric refactorization on the device (same pattern, new values of Ã): the CSR position of
+  // each CSC entry, the position in Aval of Ã(row, column) for each CSC entry (−1 for fill) and of
+  // each diagonal, and the supernodes grouped by level (leaves first).
+  std::vector<int32_t> cscToCsr, aPosCsc, aPosDiag, snLevelPtr, snByLevel;
+  int32_t maxRowLen = 0;
 };
 
 // Nested-dissection tree produced with an ordering: supernode ranges in elimination order.
@@ -105,6 +111,10 @@ std::vector<int32_t> chooseGroupWidths(const Factor& f, int teamCtas, double lat
 std::vector<int32_t> chooseGroupWidths32(const Factor& f, int ctaThreads, int ctas = 1, double latencyScale = 1.0);
 // Fills the mixed-precision fields of a factorized Factor (needs the supernodal fields).
 void buildMixed(Factor& f, const ScalarMatrix& A);
+// Fills the refactorization maps of a factor whose supernodal and mixed fields are built.
+void buildRefactorMaps(Factor& f);
+// Ã's values in elimination order (Aval) for a matrix with the pattern buildMixed saw.
+void refreshAval(Factor& f, const ScalarMatrix& A);
 
 // Up-looking LDLᵀ (Davis' LDL algorithm, as in Eigen's SimplicialLDLT). Returns false on a zero pivot.
 bool factorize(const ScalarMatrix& L, const std::vector<int32_t>& perm, Factor& f, std::string* err);
