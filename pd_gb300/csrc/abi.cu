@@ -832,6 +832,7 @@ struct pd_sim {
     r.aPosDiag = reinterpret_cast<const int32_t*>(P(I.oAPosDiag));
     r.Aval = reinterpret_cast<const double*>(P(I.oAval));
     r.snStart = reinterpret_cast<const int32_t*>(P(I.oSnStart));
+    r.rowSn = reinterpret_cast<const int32_t*>(P(I.oRowSn));
     r.offEnd = reinterpret_cast<const int32_t*>(P(I.oOffEnd));
     r.snInvOff = reinterpret_cast<const int64_t*>(P(I.oSnInv));
     r.invL = reinterpret_cast<double*>(P(I.oInvL));
@@ -846,9 +847,13 @@ struct pd_sim {
     cudaError_t e = cudaMemsetAsync(dStatus, 0, sizeof(int), stream);
     const int levels = static_cast<int>(F.snLevelPtr.size()) - 1;
     const int ns = static_cast<int>(F.snStart.size()) - 1;
+    int maxSn = 0;
+    for (int t = 0; t < ns; ++t) maxSn = std::max(maxSn, F.snStart[t + 1] - F.snStart[t]);
     if (e == cudaSuccess)
       e = static_cast<cudaError_t>(pdg::launchRefactor(r, reinterpret_cast<const int32_t*>(P(I.oSnByLevel)),
-                                                       F.snLevelPtr.data(), levels, ns, stream));
+                                                       F.snLevelPtr.data(),
+                                                       reinterpret_cast<const int32_t*>(P(I.oLvlRows)),
+                                                       F.lvlRowPtr.data(), levels, ns, maxSn, stream));
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, dStatus, sizeof(int), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     cudaFree(dStatus);

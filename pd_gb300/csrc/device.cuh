@@ -225,6 +225,7 @@ struct RefactorDev {
   const int32_t* aPosDiag;
   const double* Aval;      // Ã in elimination order (CSR)
   const int32_t* snStart;
+  const int32_t* rowSn;
   const int32_t* offEnd;
   const int64_t* snInvOff;
   double* invL;
@@ -238,10 +239,12 @@ struct RefactorDev {
 };
 // Shared memory of one level launch for rows of up to maxRowLen entries.
 int refactorSmemBytes(int maxRowLen);
-// LDLᵀ values level by level (supernodes dSnByLevel[snLevelPtr[l] .. snLevelPtr[l+1]) per launch;
-// snLevelPtr is a host array), then the block inverses of the ns supernodes and the FP32 copies.
-int launchRefactor(const RefactorDev& r, const int32_t* dSnByLevel, const int32_t* snLevelPtr, int levels, int ns,
-                   void* stream);
+// LDLᵀ values level by level — the columns dLvlRows[lvlRowPtr[l] .. lvlRowPtr[l+1]) and the
+// supernodes dSnByLevel[snLevelPtr[l] .. snLevelPtr[l+1]) of level l (the pointers into them are
+// host arrays) — then the block inverses of the ns supernodes (maxSn: the largest) and the FP32
+// copies.
+int launchRefactor(const RefactorDev& r, const int32_t* dSnByLevel, const int32_t* snLevelPtr, const int32_t* dLvlRows,
+                   const int32_t* lvlRowPtr, int levels, int ns, int maxSn, void* stream);
 
 // One instance's state in the caller's page-locked host arrays (device-visible addresses) and in
 // the arena (state_copy.cu).
