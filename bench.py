@@ -95,6 +95,18 @@ def dist_env():
     return rank, world, local
 
 
+def replica_rate(units_per_rank, seconds, world, device=None):
+    """Whole-job rate of `world` replicas that each processed `units_per_rank` units in `seconds`
+    (this rank's time): the slowest rank sets it (MAX over ranks; the replicas exchange nothing
+    else). Returns (rate, max seconds)."""
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    t_max = float(t.item())
+    return world * units_per_rank / t_max, t_max
+
+
 def workload(name, batch_count, precision="mixed"):
     import copy
     from pd_gb300 import workloads as W
@@ -461,12 +473,8 @@ def run_ours(args):
         iters_used.append(int(it[0]))
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     kernel_ms = ms / args.steps
-    t_local = torch.tensor([ms / 1e3], device="cuda", dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
-    t_max = float(t_local.item())
     count = len(scenes)
-    value = world * count * args.steps / t_max  # aggregate (cloth-)substeps/s
+    value, t_max = replica_rate(count * args.steps, ms / 1e3, world, "cuda")  # aggregate (cloth-)substeps/s
 
     # ---- e2e: through the C ABI's host-state call (pd_sim_step_host): every step copies every
     # cloth's positions and velocities in from pinned host memory, runs the substep and copies
@@ -491,10 +499,7 @@ def run_ours(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     h2d = d2h = sum(2 * 24 * sc.n for sc in scenes)
-    e_local = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(e_local, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world * count * args.steps / float(e_local.item())
+    e2e_value, _ = replica_rate(count * args.steps, e2e_s, world, "cuda")
 
     # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
     # error of this mode against the FP64 CPU oracle after the workload's full substep count
