@@ -442,12 +442,24 @@ std::vector<double> chebWeights(const pd_scene_config& c) {
   return w;
 }
 
+// Failure-path test hook of the team kernel: PD_GB300_TEST_WITHHOLD_RANK=r makes CTA r withhold
+// its first exchange-A partial, so the team's bounded waits run out (the launch then fails with
+// PD_ERR_CUDA and the exchange words are reset). Read when the descriptors are written; unset: −1.
+int32_t withholdRankForTests() {
+  const char* env = std::getenv("PD_GB300_TEST_WITHHOLD_RANK");
+  if (!env || !env[0]) return -1;
+  char* end = nullptr;
+  const long r = std::strtol(env, &end, 10);
+  return (end && *end == 0 && r >= 0 && r < 1024) ? static_cast<int32_t>(r) : -1;
+}
+
 pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog,
                           const double* omega, double* resTrace) {
   auto P = [&](size_t off) { return base + off; };
   const auto& c = I.cfg;
   const auto& s = I.scene;
   pdg::InstanceDev d{};
+  d.withholdRank = withholdRankForTests();
   d.n = s.n;
   d.ne = static_cast<int32_t>(s.edges.size());
   d.nb = static_cast<int32_t>(s.bends.size());

@@ -117,6 +117,9 @@ struct InstanceDev {
   uint32_t* epoch;             // last exchange epoch of the previous launch
   const int32_t* window;       // 2 × team: vertex range [lo, hi) whose positions a CTA reads
   int32_t* err;                // set when an exchange gave up waiting
+  int32_t withholdRank;        // failure-path test hook, −1 otherwise: this CTA of the team withholds
+                               // its exchange-A partial in the first iteration of a launch, so the
+                               // team's bounded waits run out and report through err
   // statistics
   double* resTrace;      // null, or per substep of the current launch maxIter values: the gate's
                          // residual after each iteration (NaN for iterations not run)

@@ -337,7 +337,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         if (lane == 0) {
           float pm = 0.f;
           for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
-          storeRelaxed(ptagA + kPartStride * rank, tagged(tagA, pm));
+          if (!(I.withholdRank == rank && step == 0 && k == 0))
+            storeRelaxed(ptagA + kPartStride * rank, tagged(tagA, pm));
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
