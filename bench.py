@@ -14,7 +14,9 @@ step. Beside them: ``pos_err`` (the mode's position error against the FP64 CPU o
 workload's full substep count), ``fp64_gpu`` (the plain one-cloth-per-launch FP64 GPU path on the
 same workload) and ``cpu_baseline``. ``--impl reference`` times the CPU oracle (the reference
 algorithm restated) on all host cores instead. Under torchrun each rank steps its own cloth(s)
-(replicas; no collective on the data path) and rank 0 reports the aggregate.
+(replicas; no collective on the data path) and rank 0 reports the aggregate. The default run
+(N = 1) also carries the metric's other two parts, ``batch512`` (``--workload batch``) and
+``gradients`` (``--workload differentiable``), measured by this script as child processes.
 """
 from __future__ import annotations
 
@@ -78,6 +80,7 @@ def parse():
     p.add_argument("--no-cheb", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-refactor", action="store_true")
+    p.add_argument("--no-headline-parts", action="store_true")  # skip the batch / gradient children
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--grad-side", type=int, default=64)         # smaller only for profiling captures
@@ -419,6 +422,28 @@ def position_error(P, args, scenes, cfgs, substeps, plan=None):
             "cloths": errs, "against": "FP64 CPU oracle (reference algorithm restated), cloths of the run as timed"}
 
 
+def headline_parts(args):
+    """The other two parts of the metric (the 512-cloth batch and grads/s), each measured by this
+    script as a child process on the same GPU after the single-cloth line: their key numbers for
+    the default run's JSON line. A part that fails is reported with its error."""
+    parts = {}
+    runs = {"batch512": ["--workload", "batch", "--steps", "30", "--no-cpu-baseline"],
+            "gradients": ["--workload", "differentiable", "--steps", "1", "--no-cpu-baseline"]}
+    for name, extra in runs.items():
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--warmup", str(args.warmup)] + extra
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, env=dict(os.environ))
+            line = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+        except Exception as e:  # noqa: BLE001 — reported in the line, the main result stands
+            parts[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+            continue
+        keep = ("value", "unit", "ms_per_step", "e2e", "roofline", "pos_err", "fp64_gpu", "fp64_gpu_batched",
+                "grad_check", "fp64", "cpu_baseline", "clocks", "config", "plan", "autotune")
+        parts[name] = {k: line[k] for k in keep if k in line}
+        parts[name]["command"] = " ".join(["python", "bench.py", "--warmup", str(args.warmup)] + extra)
+    return parts
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -557,6 +582,9 @@ def run_ours(args):
             line["chebyshev"] = chebyshev_line(P, args, stream, flush)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(scenes, cfgs, sub, args.cpu_sample_seconds)
+        if args.workload == "cloth40_full" and world == 1 and not args.no_headline_parts:
+            del sim  # free the device before the children run
+            line.update(headline_parts(args))
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
