@@ -57,7 +57,7 @@ def kernel_name(info):
         return "substepDenseClusterKernel"
     if kind == 4:
         return "substepDeltaKernel"
-    return "substepCorrClusterKernel" if ctas > 1 else "substepCorrKernel"
+    return "substepCorrGridKernel" if ctas > 16 else "substepCorrClusterKernel" if ctas > 1 else "substepCorrKernel"
 
 
 UNIT = "substeps/s"

@@ -168,6 +168,10 @@ int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, in
 int launchSubstepCorrCluster(const InstanceDev* dInstances, int count, int cs, int substeps, void* stream);
 // `cs` if a cluster of that many correction-kernel CTAs can run on this device, else 0.
 int corrClusterSupported(int cs);
+// One cloth (dInstances[0]) by `ctas` co-resident CTAs on a cooperative launch: the cluster code
+// with grid barriers. corrGridCapacity: the most CTAs such a launch can hold on this device.
+int launchSubstepCorrGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream);
+int corrGridCapacity();
 constexpr int kDeltaThreads = 512;
 
 // Work arrays of one gradient problem (adjoint.cu): the loss is the mean over free vertices of

@@ -373,6 +373,19 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const 
   runSubstepsCorr<true>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
+// One large cloth on a cooperative grid of CTAs (more SMs than a cluster holds): the cluster code
+// path with grid barriers; the instance's FP64 solve workspace (unused by the correction kernels)
+// holds the per-CTA slots of the team maxima.
+__global__ void __launch_bounds__(kBlockThreads) substepCorrGridKernel(const InstanceDev* __restrict__ insts,
+                                                                      int substeps) {
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  const InstanceDev& I = insts[0];
+  Team<true> tm{static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x)};
+  tm.gslots = I.w;
+  runSubstepsCorr<true>(I, tm, substeps, I.y32, I.t32, red, slots);
+}
+
 cudaLaunchConfig_t corrClusterConfig(int blocks, int cs, void* stream, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
@@ -410,6 +423,35 @@ int corrClusterSupported(int cs) {
   const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, substepCorrClusterKernel, &cfg);
   if (e != cudaSuccess) cudaGetLastError();
   return (e == cudaSuccess && clusters > 0) ? cs : 0;
+}
+
+int corrGridCapacity() {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  int dev = 0, sms = 0, perSm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepCorrGridKernel, kBlockThreads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return cached = 0;
+  }
+  return cached = perSm * sms;
+}
+
+int launchSubstepCorrGrid(const InstanceDev* d, int ctas, int substeps, void* stream) {
+  if (substeps <= 0) return 0;
+  if (ctas < 2 || ctas > corrGridCapacity()) return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepCorrGridKernel, d, substeps);
+  return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 
 int launchSubstepCorrCluster(const InstanceDev* d, int count, int cs, int substeps, void* stream) {

@@ -19,11 +19,18 @@ template <bool CLUSTER>
 struct Team {
   int rank;  // CTA rank in the cluster
   int size;  // CTAs in the cluster
+  // A grid team (one cloth on a cooperative launch of many CTAs, CLUSTER = true): 2 × size doubles
+  // of global memory for the team maximum; null for a cluster. Barriers are then grid barriers.
+  double* gslots = nullptr;
   __device__ __forceinline__ int tid() const { return rank * (int)blockDim.x + (int)threadIdx.x; }
   __device__ __forceinline__ int count() const { return size * (int)blockDim.x; }
   __device__ __forceinline__ void sync() const {
-    if (CLUSTER) cooperative_groups::this_cluster().sync();
-    else __syncthreads();
+    if (CLUSTER) {
+      if (gslots) cooperative_groups::this_grid().sync();
+      else cooperative_groups::this_cluster().sync();
+    } else {
+      __syncthreads();
+    }
   }
   // loads of data another CTA of the cluster may have written since the last barrier
   template <class T>
@@ -39,6 +46,15 @@ template <bool CLUSTER>
 __device__ __forceinline__ double teamMax(const Team<CLUSTER>& tm, double v, double* red, double* slots, int& parity) {
   v = blockMax(v, red);
   if (!CLUSTER) return v;
+  if (tm.gslots) {  // grid team: one slot per CTA in global memory, two buffers by parity
+    double* g = tm.gslots + parity * tm.size;
+    parity ^= 1;
+    if (threadIdx.x == 0) g[tm.rank] = v;
+    cooperative_groups::this_grid().sync();
+    double m = 0.0;
+    for (int r = threadIdx.x; r < tm.size; r += blockDim.x) m = fmax(m, __ldcg(g + r));
+    return blockMax(m, red);
+  }
   double* slot = slots + parity;
   parity ^= 1;
   if (threadIdx.x == 0) *slot = v;

@@ -1,0 +1,65 @@
+"""One MIXED cloth above the explicit-inverse limit on a cooperative grid of CTAs (the correction
+kernel's cluster code with grid barriers, plan team_ctas > 16): against the oracle with the residual
+gate, the displacement gate and Chebyshev-weighted iterates, and among the autotuner's candidates.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from pd_gb300 import workloads as W
+from tests.helpers import max_rel, oracle_twin
+
+pytestmark = pytest.mark.gpu
+
+
+def big_cfg(**kw):
+    c = W._base(grid_nx=70, grid_ny=64, grid_spacing=1 / 69, max_iterations=12, shear_stiffness=900.0,
+                bend_stiffness=40.0)
+    c = copy.copy(c)
+    c.precision = 4
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+@pytest.mark.parametrize("gate", ["residual", "displacement", "chebyshev"])
+def test_grid_team_matches_oracle(pdg, gate):
+    kw = {"residual": {}, "displacement": {"residual_tolerance": 0.0, "rel_tolerance": 1e-3},
+          "chebyshev": {"cheb_mode": pdg.PD_CHEB_RHO, "cheb_start": 4, "residual_tolerance": 1e-6}}[gate]
+    cfg = big_cfg(**kw)
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    sim.set_plan({"team_ctas": 152})
+    info = sim.info()
+    assert info["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32_CORRECTION and info["cluster_ctas"] == 152
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    sim.step(30)
+    its_o, _ = orc.step(30)
+    assert max_rel(sim.state()[0], orc.state()[0]) <= 1e-5
+    its_g, _ = sim.iteration_log()
+    assert np.mean(its_g == its_o) >= 0.9
+
+
+def test_grid_team_repeated_launches_and_largest_team(pdg):
+    """Many launches of one substep each (the barrier state carries over between launches), on
+    the largest team the device holds."""
+    cfg = big_cfg()
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    sim.set_plan({"team_ctas": 1024})  # capped at the device's cooperative capacity
+    ctas = sim.info()["cluster_ctas"]
+    assert ctas > 16
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    for _ in range(12):
+        sim.step(1)
+    orc.step(12)
+    assert max_rel(sim.state()[0], orc.state()[0]) <= 1e-5
+
+
+def test_autotuner_tries_grid_teams(pdg):
+    cfg = big_cfg(max_iterations=6)
+    sim = pdg.Simulator(pdg.make_grid(cfg), cfg)
+    rep = sim.autotune(2)
+    assert any(t["team_ctas"] > 16 for t in rep["tried"])
+    assert rep["ms"][rep["chosen"]] == min(rep["ms"])
