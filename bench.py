@@ -50,7 +50,7 @@ def kernel_name(info):
     if kind == 0:
         return "substepExactKernel"
     if kind == 1:
-        return "substepClusterKernel" if ctas > 1 else "substepFastKernel"
+        return "substepGridKernel" if ctas > 16 else "substepClusterKernel" if ctas > 1 else "substepFastKernel"
     if kind == 2:
         return "substepMixedClusterKernel" if ctas > 1 else "substepMixedKernel"
     if kind == 3:

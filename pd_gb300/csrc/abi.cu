@@ -703,6 +703,20 @@ struct pd_sim {
       const int count = static_cast<int>(inst.size());
       want = count <= 9 ? 16 : count <= 19 ? 8 : count <= 38 ? 4 : count <= 76 ? 2 : 1;
     }
+    // one large cloth: a grid team, two CTAs an SM (a 256×256 FP64 cloth: 15.6 ms a substep on 304
+    // CTAs against 97 ms on a 16-CTA cluster)
+    if (!mixedSolve(p) && inst[0].cfg.cluster_ctas <= 0 && plan.team_ctas <= 0 && inst.size() == 1 &&
+        inst[0].scene.n >= kBatchClusterMinVertices && pdg::gridCapacity() > 32)
+      want = pdg::gridCapacity() / 2;
+    if (!mixedSolve(p) && inst.size() == 1 && want > 16 && pdg::gridCapacity() > 16) {  // a grid team
+      // its team-maximum slots (2 per CTA) live in the 3n-double workspace x0
+      const int ctas = std::min({want, pdg::gridCapacity(), 3 * inst[0].scene.n / 2});
+      if (ctas > 16) {
+        teamCtas = ctas;
+        return;
+      }
+      want = 16;
+    }
     int cs = 1;
     while (cs * 2 <= std::min(want, 16)) cs *= 2;
     if (!mixedSolve(p)) {
@@ -761,7 +775,11 @@ struct pd_sim {
     if (want <= 0 && inst.size() == 1 && inst[0].scene.n >= kBatchClusterMinVertices &&
         pdg::corrGridCapacity() > 16)
       want = pdg::corrGridCapacity();
-    if (want > 16 && inst.size() == 1) return std::min(want, pdg::corrGridCapacity());  // a grid team
+    if (want > 16 && inst.size() == 1) {  // a grid team; its slots (2 per CTA) live in the 3n-double w
+      const int ctas = std::min({want, pdg::corrGridCapacity(), 3 * inst[0].scene.n / 2});
+      if (ctas > 16) return ctas;
+      want = 16;
+    }
     if (want <= 0) {
       int minN = 1 << 30;
       for (const auto& I : inst) minN = std::min(minN, I.scene.n);
@@ -1064,8 +1082,9 @@ struct pd_sim {
       rc = teamCtas > 1 ? pdg::launchSubstepMixedCluster(dDesc, count, teamCtas, smemBytes, substeps, st)
                         : pdg::launchSubstepMixed(dDesc, count, substeps, smemBytes, st);
     } else {
-      rc = teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st)
-                        : pdg::launchSubstepFast(dDesc, count, substeps, smemBytes, st);
+      rc = teamCtas > 16  ? pdg::launchSubstepGrid(dDesc, teamCtas, substeps, st)
+           : teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st)
+                          : pdg::launchSubstepFast(dDesc, count, substeps, smemBytes, st);
     }
     if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
     return PD_OK;
@@ -1881,8 +1900,8 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
         }
     } else {  // CTAs per cloth of the cluster kernels; one large MIXED cloth also on a grid of CTAs
       std::vector<int> sizes = count <= 9 ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{1, 2, 4};
-      if (corr && count == 1) {
-        const int cap = pdg::corrGridCapacity();
+      if ((corr || supernodalFp64(p)) && count == 1) {
+        const int cap = corr ? pdg::corrGridCapacity() : pdg::gridCapacity();
         for (int g : {cap / 4, cap / 2, cap})
           if (g > 16) sizes.push_back(g);
       }
@@ -2085,8 +2104,8 @@ int pd_sim_gradient(pd_sim* s, int32_t substeps, const double* const* targets, c
     rc = cudaFail(cudaGetLastError(), "gradient descriptors");
   if (rc == PD_OK) {
     // a cluster per problem where the FP64 path runs clusters (the planner's CTAs per cloth)
-    int cs = supernodalFp64(s->precision()) ? s->teamCtas : 1;
-    if (cs > 1 && pdg::gradClusterSupported(cs) != cs) cs = 1;
+    int cs = supernodalFp64(s->precision()) ? std::min(s->teamCtas, 16) : 1;  // a grid team: a 16-CTA cluster
+    while (cs > 1 && pdg::gradClusterSupported(cs) != cs) cs /= 2;
     const int lrc = pdg::launchGradient(s->dDesc, dG, count, cs, substeps, smem, s->stream);
     if (lrc != 0) rc = cudaFail(static_cast<cudaError_t>(lrc), "gradient launch");
   }

@@ -144,6 +144,10 @@ int launchSolveFast(const InstanceDev* dInstance, const double* b, double* x, in
 int launchSubstepCluster(const InstanceDev* dInstances, int count, int clusterSize, int substeps, void* stream);
 // `want` if a cluster of that many 256-thread CTAs can run on this device, else 0.
 int clusterSizeSupported(int want);
+// One cloth (dInstances[0]) of the FP64 supernodal substep by `ctas` co-resident CTAs on a
+// cooperative launch (the cluster code with grid barriers); gridCapacity: the most CTAs it holds.
+int launchSubstepGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream);
+int gridCapacity();
 // Mixed-precision substep (FP32 solve + one FP64 refinement step): one CTA per instance with
 // smemBytes of workspace (72·n when it fits, else 0 = global), or a cluster of clusterSize CTAs
 // per instance, each CTA solving the whole system in its own shared memory (72·max n bytes).

@@ -40,6 +40,18 @@ __global__ void __launch_bounds__(kBlockThreads) substepClusterKernel(const Inst
   runSubstepsTeam<true>(I, tm, substeps, I.w, I.tbuf, red, slots);
 }
 
+// One large cloth on a cooperative grid of CTAs: the cluster code with grid barriers; the
+// instance's FP64 refinement workspace x0 (unused in the FP64 modes) holds the team-maximum slots.
+__global__ void __launch_bounds__(kBlockThreads) substepGridKernel(const InstanceDev* __restrict__ insts,
+                                                                   int substeps) {
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  const InstanceDev& I = insts[0];
+  Team<true> tm{static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x)};
+  tm.gslots = I.x0;
+  runSubstepsTeam<true>(I, tm, substeps, I.w, I.tbuf, red, slots);
+}
+
 __global__ void __launch_bounds__(kBlockThreads) solveFastKernel(const InstanceDev* __restrict__ inst,
                                                                  const double* __restrict__ b,
                                                                  double* __restrict__ x, int smemBytes) {
@@ -127,6 +139,35 @@ int clusterSizeSupported(int want) {
   if (e != cudaSuccess) cudaGetLastError();
   cached[want] = (e == cudaSuccess && clusters > 0) ? 1 : -1;
   return cached[want] > 0 ? want : 0;
+}
+
+int gridCapacity() {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  int dev = 0, sms = 0, perSm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepGridKernel, kBlockThreads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return cached = 0;
+  }
+  return cached = perSm * sms;
+}
+
+int launchSubstepGrid(const InstanceDev* d, int ctas, int substeps, void* stream) {
+  if (substeps <= 0) return 0;
+  if (ctas < 2 || ctas > gridCapacity()) return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.stream = static_cast<cudaStream_t>(stream);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepGridKernel, d, substeps);
+  return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 
 int launchSubstepCluster(const InstanceDev* d, int count, int clusterSize, int substeps, void* stream) {

@@ -63,3 +63,36 @@ def test_autotuner_tries_grid_teams(pdg):
     rep = sim.autotune(2)
     assert any(t["team_ctas"] > 16 for t in rep["tried"])
     assert rep["ms"][rep["chosen"]] == min(rep["ms"])
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_fp64_supernodal_grid_team_matches_oracle(pdg, p):
+    """The FP64 supernodal kernel (FP64 and FP32-projection modes) on a grid team."""
+    cfg = copy.copy(W._base(grid_nx=60, grid_ny=60, grid_spacing=1 / 59, max_iterations=12, shear_stiffness=1000.0,
+                            bend_stiffness=50.0))
+    cfg.precision = p
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    sim.set_plan({"team_ctas": 152})
+    assert sim.info()["cluster_ctas"] == 152 and sim.info()["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    sim.step(25)
+    its_o, _ = orc.step(25)
+    assert max_rel(sim.state()[0], orc.state()[0]) <= (1e-10 if p == 1 else 1e-5)
+    assert np.array_equal(sim.iteration_log()[0], its_o) or p == 2
+
+
+def test_grid_team_is_capped_by_its_slot_workspace(pdg):
+    """A grid team keeps two slots per CTA in a 3n-double workspace: an 8×6 cloth (48 vertices)
+    takes at most 72 CTAs, a 3×3 cloth keeps a cluster; both step like the oracle."""
+    for (nx, ny), cap in (((8, 6), 72), ((3, 3), 16)):
+        cfg = copy.copy(W._base(grid_nx=nx, grid_ny=ny, grid_spacing=0.05, max_iterations=4))
+        cfg.precision = 1
+        scene = pdg.make_grid(cfg)
+        sim = pdg.Simulator(scene, cfg)
+        sim.set_plan({"team_ctas": 300})
+        assert sim.info()["cluster_ctas"] <= cap
+        orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+        sim.step(3)
+        orc.step(3)
+        assert max_rel(sim.state()[0], orc.state()[0]) <= 1e-10
