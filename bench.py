@@ -402,6 +402,22 @@ def refactor_times(P, scenes, cfgs):
     return out
 
 
+def stage_shares(P, scenes, cfgs, plan, substeps=20):
+    """Where a substep's time goes (StageTimes, core/sim/Scene.h:140-149): device stage times of
+    cloth 0 over `substeps` substeps on a separate handle with the timed plan, as shares of the
+    total, beside the total per substep."""
+    sim = P.Simulator(scenes, cfgs)
+    sim.set_plan(plan)
+    sim.set_stage_timing(True)
+    sim.step(substeps)
+    t = sim.stage_times(0)
+    total = t["total"]
+    keys = ("predict", "local_step", "scatter", "solve", "unpack_scan", "velocity")
+    out = {k: (t[k] / total if total > 0 else 0.0) for k in keys}
+    out["ms_per_substep"] = total / substeps * 1e3
+    return out
+
+
 def position_error(P, args, scenes, cfgs, substeps, plan=None):
     """max |x_gpu − x_oracle| / max |x_oracle| after `substeps` substeps from the initial state, this
     precision mode against the FP64 CPU oracle, for the run as timed: every cloth on one handle with
@@ -528,10 +544,11 @@ def run_ours(args):
 
     # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
     # error of this mode against the FP64 CPU oracle after the workload's full substep count
-    fp64_line = pos_err = refactor = None
+    fp64_line = pos_err = refactor = stages = None
     if rank == 0:
         if len(scenes) == 1 and not args.no_refactor:
             refactor = refactor_times(P, scenes, cfgs)
+        stages = stage_shares(P, scenes, cfgs, plan) if len(scenes) == 1 else None
         if not args.no_fp64_gpu:
             fp64_line = (time_fp64_one_at_a_time(P, args) if len(scenes) > 1
                          else time_fp64_gpu(P, args, stream, flush))
@@ -562,7 +579,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "pd_sim_step_host (gather kernel, substep, scatter kernel: one CUDA graph)"
                         if info["host_state"] == P.PD_HOST_STATE_GRAPH else "pd_sim_step_host (cudaMemcpyAsync per array)"},
-                "clocks": clocks, "plan": plan, "autotune": tune, "refactor": refactor}
+                "clocks": clocks, "plan": plan, "autotune": tune, "refactor": refactor, "stages": stages}
         if PRECISIONS[args.precision][0] <= 1:
             ops = sum(fp64_ops(s, sim.info(i)["factor_nnz"], iters_used[i]) for i, s in enumerate(scenes))
             fp64_peak = 503.4  # Gop/s, measured DMUL/DADD/DFMA issue rate on this GPU

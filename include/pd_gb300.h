@@ -254,6 +254,23 @@ int pd_sim_device_state(pd_sim* s, int32_t instance, double** positions, double*
 int pd_sim_bind_host(pd_sim* s, double* const* positions, double* const* velocities);
 int pd_sim_step_host(pd_sim* s, int32_t substeps);
 
+/* ---- Stage times: StageTimes (core/sim/Scene.h:140-149) and resetStageTimes (core/sim/Integrator.h:20) ----
+ * Seconds accumulated over the substeps stepped while timing is on (off by default). The device
+ * stages are timed by one thread of the cloth's first CTA with the GPU's global timer at the
+ * barriers that close each stage, so they sum to `total`: predict; local_step (projections — the
+ * MIXED kernels' fused correction pass, which also scatters); scatter (the colour-ordered gather
+ * of b; 0 where fused); solve (the triangular solves, or the team kernel's exchange of the
+ * correction and its rows of Ã⁻¹); unpack_scan (unpack, the displacement / residual scan and the
+ * gate; the team kernel's update and position exchange); velocity. `assemble` is host wall time
+ * of the (re)factorizations of this instance, device refactorizations and re-uploads included.
+ * Timing slows nothing measurable: one thread reads a clock a few times per iteration. */
+typedef struct pd_stage_times {
+  double predict, local_step, scatter, assemble, solve, unpack_scan, velocity, total;
+} pd_stage_times;
+int pd_sim_set_stage_timing(pd_sim* s, int32_t enable);
+int pd_sim_get_stage_times(pd_sim* s, int32_t instance, pd_stage_times* out);
+int pd_sim_reset_stage_times(pd_sim* s);
+
 /* ---- Spectrum of the linearised PD iteration (the reference's _verify/iteration_spectrum.cpp) ----
  * At instance i's current positions: T = I − A⁻¹(M/h² + N + K_b), N = Σ_e κ_e A_eᵀ(n_e n_eᵀ)A_e with
  * n_e = unit(x_a − x_b), K_b = Σ_s k·A_sᵀA_s (bending stencils, whose projection is constant; the

@@ -165,12 +165,20 @@ inline Mesh makeGridMesh(const SceneConfig& cfg) {
   return m;
 }
 
+// core/sim/Scene.h:140-149, in seconds (see pd_sim_set_stage_timing for what each stage covers
+// on the GPU).
+struct StageTimes {
+  double predict = 0.0, localStep = 0.0, scatter = 0.0, assemble = 0.0, solve = 0.0, unpackScan = 0.0,
+         velocity = 0.0, total = 0.0;
+};
+
 // core/sim/Scene.h:151-192: the configuration, the mesh (the state of record, on the host) and the
 // counters stepOnce maintains; the GPU copy of the scene lives in the pd_sim handle.
 class SimContext {
  public:
   SceneConfig config;
   Mesh mesh;
+  StageTimes times;  // filled while stage timing is on (setStageTiming)
   int factorizeCount = 0;
   int iterationsUsed = 0;
   int earlyExitCount = 0;
@@ -203,6 +211,8 @@ class SimContext {
       lastPinned_ = std::move(o.lastPinned_);
       lastPins_ = std::move(o.lastPins_);
       lastCfg_ = o.lastCfg_;
+      times = o.times;
+      timing_ = o.timing_;
       boundX_ = boundV_ = nullptr;  // re-bound at the next step
     }
     return *this;
@@ -210,6 +220,11 @@ class SimContext {
   ~SimContext() { release(); }
 
   pd_sim* handle() const { return h_; }
+
+  void setStageTiming(bool on) {
+    check(pd_sim_set_stage_timing(h_, on ? 1 : 0));
+    timing_ = on;
+  }
 
   // What the reference's stepOnce reads from the context at each substep: edits of the pin
   // targets go to the GPU as RHS changes; edits of the stiffnesses, the pin mask or dt refactorize
@@ -314,6 +329,11 @@ class SimContext {
     earlyExitCount = st.early_exit_count;
     lastResidual = st.last_residual;
     factorizeCount = info.factorize_count;
+    if (timing_) {
+      pd_stage_times t{};
+      check(pd_sim_get_stage_times(h_, 0, &t));
+      times = StageTimes{t.predict, t.local_step, t.scatter, t.assemble, t.solve, t.unpack_scan, t.velocity, t.total};
+    }
   }
   void release() {
     if (h_) pd_sim_destroy(h_);
@@ -321,6 +341,7 @@ class SimContext {
   }
 
   pd_sim* h_ = nullptr;
+  bool timing_ = false;
   double* boundX_ = nullptr;
   double* boundV_ = nullptr;
   std::vector<double> lastK_;
@@ -334,6 +355,12 @@ inline SimContext makeScene(const SceneConfig& config) { return SimContext(makeG
 
 // core/sim/Integrator.h:14: one substep; returns the PD iterations used.
 inline int stepOnce(SimContext& ctx) { return ctx.step(); }
+
+// core/sim/Integrator.h:20
+inline void resetStageTimes(SimContext& ctx) {
+  check(pd_sim_reset_stage_times(ctx.handle()));
+  ctx.times = StageTimes{};
+}
 
 // core/sim/Integrator.h:17: substepsPerFrame substeps.
 inline void stepFrame(SimContext& ctx) {

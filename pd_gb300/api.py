@@ -97,6 +97,11 @@ class _Spectrum(C.Structure):
                 ("lambda_max_prev", C.c_double), ("lambda_min", C.c_double), ("rho_cheb", C.c_double)]
 
 
+class _StageTimes(C.Structure):
+    _fields_ = [(f, C.c_double) for f in ("predict", "local_step", "scatter", "assemble", "solve", "unpack_scan",
+                                           "velocity", "total")]
+
+
 class _SimStats(C.Structure):
     _fields_ = [("iterations_used", C.c_int32), ("converged", C.c_int32),
                 ("early_exit_count", C.c_int32), ("last_residual", C.c_double)]
@@ -142,6 +147,9 @@ _SIGS = {
     "pd_sim_set_state": ([C.c_void_p, C.c_int32, _dp, _dp], C.c_int),
     "pd_sim_device_state": ([C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)], C.c_int),
     "pd_sim_bind_host": ([C.c_void_p, C.POINTER(_dp), C.POINTER(_dp)], C.c_int),
+    "pd_sim_set_stage_timing": ([C.c_void_p, C.c_int32], C.c_int),
+    "pd_sim_get_stage_times": ([C.c_void_p, C.c_int32, C.POINTER(_StageTimes)], C.c_int),
+    "pd_sim_reset_stage_times": ([C.c_void_p], C.c_int),
     "pd_sim_spectrum": ([C.c_void_p, C.c_int32, C.c_int32, C.POINTER(_Spectrum)], C.c_int),
     "pd_sim_autotune": ([C.c_void_p, C.c_int32, C.POINTER(_Plan), _dp, _ip, _ip], C.c_int),
     "pd_sim_set_plan": ([C.c_void_p, C.POINTER(_Plan)], C.c_int),
@@ -449,6 +457,18 @@ class Simulator:
         _check(self._lib.pd_sim_step_host(self._h, int(substeps)))
         if substeps > 0:
             self._last = int(substeps)
+
+    def set_stage_timing(self, enable: bool = True):
+        """StageTimes (core/sim/Scene.h:140-149) on the device: see pd_sim_set_stage_timing."""
+        _check(self._lib.pd_sim_set_stage_timing(self._h, int(bool(enable))))
+
+    def stage_times(self, i: int = 0) -> dict:
+        out = _StageTimes()
+        _check(self._lib.pd_sim_get_stage_times(self._h, i, C.byref(out)))
+        return {f: getattr(out, f) for f, _ in _StageTimes._fields_}
+
+    def reset_stage_times(self):
+        _check(self._lib.pd_sim_reset_stage_times(self._h))
 
     def spectrum(self, i: int = 0, iters: int = 400) -> dict:
         """Power-iteration spectrum of the linearised PD map of instance i at its current positions

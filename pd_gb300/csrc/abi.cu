@@ -99,6 +99,7 @@ struct Instance {
       oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl, oXhl,
       oXhatHl, oD, oCscToCsr, oAPosCsc, oAPosDiag, oSnByLevel;
   bool gpuRefactor = false;   // the next upload computes the factor's values on the device
+  double assembleSeconds = 0.0;  // StageTimes::assemble: (re)factorizations, host and device
   int deviceRefactorCount = 0;
   std::vector<int32_t> patRowptr, patCol;  // pattern of Ã the current symbolic factor was built for
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
@@ -454,12 +455,13 @@ int32_t withholdRankForTests() {
 }
 
 pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, uint8_t* convLog,
-                          const double* omega, double* resTrace) {
+                          const double* omega, double* resTrace, double* stageNs) {
   auto P = [&](size_t off) { return base + off; };
   const auto& c = I.cfg;
   const auto& s = I.scene;
   pdg::InstanceDev d{};
   d.withholdRank = withholdRankForTests();
+  d.stageNs = stageNs;
   d.n = s.n;
   d.ne = static_cast<int32_t>(s.edges.size());
   d.nb = static_cast<int32_t>(s.bends.size());
@@ -620,6 +622,8 @@ struct pd_sim {
   cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
   cudaEvent_t forkEv = nullptr, joinEv = nullptr;
   unsigned generation = 0;      // bumped whenever the arena, the descriptors or the plan change
+  bool stageTiming = false;     // the substep kernels time their stages (StageTimes)
+  double* dStage = nullptr;     // kStageCount ns accumulators per instance, kept across uploads
   pd_plan plan{};               // overrides of the planner's choices (pd_sim_set_plan / pd_sim_autotune)
   int bigCs = kBatchCluster;    // CTAs per large cloth of a MIXED batch on the second stream
   // host-state stepping (pd_sim_bind_host / pd_sim_step_host)
@@ -642,6 +646,7 @@ struct pd_sim {
     dropGraph();
     if (dHostTable) cudaFree(dHostTable);
     if (hStatus) cudaFreeHost(hStatus);
+    if (dStage) cudaFree(dStage);
     if (ownStream) cudaStreamDestroy(ownStream);
   }
   void dropGraph() {
@@ -961,7 +966,8 @@ struct pd_sim {
     }
     for (size_t i = 0; i < inst.size(); ++i) {
       desc.push_back(describe(inst[i], dArena, dIterLog + i * logCapacity, dConvLog + i * logCapacity,
-                              dOmega ? dOmega + wOff[i] : nullptr, traceOn ? dTrace + traceOff[i] : nullptr));
+                              dOmega ? dOmega + wOff[i] : nullptr, traceOn ? dTrace + traceOff[i] : nullptr,
+                              stageTiming ? dStage + pdg::kStageCount * i : nullptr));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
       int rows = 0;
       const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
@@ -1371,7 +1377,9 @@ int pd_sim_create_batch(int32_t count, const pd_mesh* meshes, const pd_scene_con
     std::string err = pdg::validateScene(I.scene);
     if (!err.empty()) return fail(PD_ERR_INVALID_ARGUMENT, "instance " + std::to_string(i) + ": " + err);
     pdg::buildTopology(I.scene, I.topo);
+    const auto t0 = Clock::now();
     err = prepare(I, true);
+    I.assembleSeconds = secondsSince(t0);
     if (!err.empty()) {
       return fail(prepareCode(err), "instance " + std::to_string(i) + ": " + err);
     }
@@ -1583,9 +1591,12 @@ static int rebuild(pd_sim* s, int i, bool reanalyze) {
   int rc = s->pullState();
   if (rc) return rc;
   Instance& I = s->inst[i];
+  const auto t0 = Clock::now();
   const std::string err = prepare(I, reanalyze);
   if (!err.empty()) return fail(prepareCode(err), err);
-  return s->upload(s->logCapacity > 0 ? s->logCapacity : 1);
+  rc = s->upload(s->logCapacity > 0 ? s->logCapacity : 1);
+  I.assembleSeconds += secondsSince(t0);
+  return rc;
 }
 
 int pd_sim_set_pin_positions(pd_sim* s, int32_t i, const double* q) {
@@ -1653,13 +1664,59 @@ int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
     int rc = s->pullState();
     if (rc) return rc;
     for (auto& I : s->inst) {
+      const auto t0 = Clock::now();
       const std::string err = prepare(I, false);
       if (!err.empty()) return fail(PD_ERR_FACTORIZATION, err);
+      I.assembleSeconds += secondsSince(t0);
     }
-    return s->upload(s->logCapacity);
+    const auto t1 = Clock::now();
+    rc = s->upload(s->logCapacity);
+    const double share = secondsSince(t1) / static_cast<double>(s->inst.size());
+    for (auto& I : s->inst) I.assembleSeconds += share;  // the re-upload (and device refactorization)
+    return rc;
   }
   if (const int rc_ = s->sync()) return rc_;
   return s->writeDescriptors();
+}
+
+// ------------------------------------------------------------------------------ stage times
+int pd_sim_set_stage_timing(pd_sim* s, int32_t enable) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (const int rc_ = s->sync()) return rc_;
+  if (enable && !s->dStage) {
+    const size_t bytes = sizeof(double) * pdg::kStageCount * s->inst.size();
+    PD_CUDA(cudaMalloc(&s->dStage, bytes));
+    PD_CUDA(cudaMemset(s->dStage, 0, bytes));
+  }
+  s->stageTiming = enable != 0;
+  return s->writeDescriptors();
+}
+
+int pd_sim_reset_stage_times(pd_sim* s) {
+  if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (const int rc_ = s->sync()) return rc_;
+  if (s->dStage) PD_CUDA(cudaMemset(s->dStage, 0, sizeof(double) * pdg::kStageCount * s->inst.size()));
+  for (auto& I : s->inst) I.assembleSeconds = 0.0;
+  return PD_OK;
+}
+
+int pd_sim_get_stage_times(pd_sim* s, int32_t i, pd_stage_times* out) {
+  int rc = checkInstance(s, i);
+  if (rc) return rc;
+  if (!out) return fail(PD_ERR_INVALID_ARGUMENT, "null output");
+  if (const int rc_ = s->sync()) return rc_;
+  double ns[pdg::kStageCount] = {0};
+  if (s->dStage)
+    PD_CUDA(cudaMemcpy(ns, s->dStage + pdg::kStageCount * static_cast<size_t>(i), sizeof(ns), cudaMemcpyDeviceToHost));
+  out->predict = ns[pdg::kStagePredict] * 1e-9;
+  out->local_step = ns[pdg::kStageLocal] * 1e-9;
+  out->scatter = ns[pdg::kStageScatter] * 1e-9;
+  out->assemble = s->inst[i].assembleSeconds;
+  out->solve = ns[pdg::kStageSolve] * 1e-9;
+  out->unpack_scan = ns[pdg::kStageUnpack] * 1e-9;
+  out->velocity = ns[pdg::kStageVelocity] * 1e-9;
+  out->total = ns[pdg::kStageTotal] * 1e-9;
+  return PD_OK;
 }
 
 int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {

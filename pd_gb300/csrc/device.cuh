@@ -121,6 +121,8 @@ struct InstanceDev {
                                // its exchange-A partial in the first iteration of a launch, so the
                                // team's bounded waits run out and report through err
   // statistics
+  double* stageNs;       // null, or the stage-time accumulators (ns) of StageTimes, rank 0's view:
+                         // predict, localStep, scatter, solve, unpackScan, velocity, total
   double* resTrace;      // null, or per substep of the current launch maxIter values: the gate's
                          // residual after each iteration (NaN for iterations not run)
   int32_t* iterLog;      // per substep of the current launch
@@ -129,6 +131,44 @@ struct InstanceDev {
   int32_t* earlyExits;   // scalar, accumulates
   int32_t* iterationsUsed;
   int32_t* converged;
+};
+
+// Stages of StageTimes (core/sim/Scene.h:140-149) timed on the device.
+enum StageIndex { kStagePredict = 0, kStageLocal, kStageScatter, kStageSolve, kStageUnpack, kStageVelocity, kStageTotal,
+                  kStageCount };
+
+// %globaltimer laps of one thread (rank 0's thread 0) into I.stageNs; nothing when stageNs is null.
+// A lap is taken right after a barrier, so the stage it closes is finished in the whole CTA. The
+// two timestamps live in shared memory (one pair per CTA of the kernel), so a kernel carries only
+// the `on` predicate in registers.
+static __shared__ unsigned long long stageStamp[2];  // start of the substep, last lap
+static __shared__ int stageOn;                        // this CTA times stages (rank 0, stageNs set)
+
+struct StageClock {
+  __device__ __forceinline__ StageClock(const InstanceDev& I, bool thread0) {
+    if (thread0) {
+      stageOn = I.stageNs != nullptr;
+      if (stageOn) stageStamp[0] = stageStamp[1] = now();
+    }
+  }
+  static __device__ __forceinline__ unsigned long long now() {
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+    return v;
+  }
+  // called by every thread; only the timing thread (the one that set stageOn) acts
+  __device__ __forceinline__ void lap(const InstanceDev& I, bool thread0, int stage) const {
+    if (!thread0 || !stageOn) return;
+    const unsigned long long n = now();
+    I.stageNs[stage] += static_cast<double>(n - stageStamp[1]);
+    stageStamp[1] = n;
+  }
+  // closes the substep at the last lap's stamp, so that the stages partition the total exactly
+  __device__ __forceinline__ void finish(const InstanceDev& I, bool thread0) const {
+    if (!thread0 || !stageOn) return;
+    I.stageNs[kStageTotal] += static_cast<double>(stageStamp[1] - stageStamp[0]);
+    stageStamp[0] = stageStamp[1];
+  }
 };
 
 // Launch the reference-order FP64 substep kernel over `count` instances.

@@ -185,6 +185,7 @@ __device__ double vertexResidual(const InstanceDev& I, const double* X, int v) {
 // solver may use `t` as a second workspace of the same size.
 template <class A, class Solve>
 __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, double* t, double* red, int* flag) {
+  const StageClock clk(I, threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict x̂ = x + h·v + h²·g, x_n = x, bBase = (M/h²)·x̂ (Integrator.cpp:447-472); the
     // displacement scale max|x̂ − x_n|∞ is the same in every iteration of the substep.
@@ -204,16 +205,21 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
     }
     scale = blockMax(scale, red);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
+    clk.lap(I, threadIdx.x == 0, kStagePredict);
 
     edgePass<A>(I, I.x, false);  // projection of x_n for the first scatter
     __syncthreads();
+    clk.lap(I, threadIdx.x == 0, kStageLocal);
     int used = 0;
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
     for (int k = 0; k < I.maxIter; ++k) {
       gatherRhs<A>(I, w);
       __syncthreads();
+      clk.lap(I, threadIdx.x == 0, kStageScatter);
       Solve::run(I, w, t);
+      __syncthreads();
+      clk.lap(I, threadIdx.x == 0, kStageSolve);
       // unpack + displacement scan (Integrator.cpp:618-663); an over-relaxed iteration puts
       // x_prev + (x_solve − x_prev)·ω and keeps x_solve for the residual (:631-641)
       const bool blend = k >= I.chebFrom;
@@ -242,9 +248,11 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
         }
       }
       __syncthreads();
+      clk.lap(I, threadIdx.x == 0, kStageUnpack);
       const double* X = split ? I.xsol : I.x;
       edgePass<A>(I, X, I.useResidual != 0);
       __syncthreads();
+      clk.lap(I, threadIdx.x == 0, kStageLocal);
       double res = 0.0;
       if (I.useResidual) {
         for (int v = threadIdx.x; v < I.n; v += blockDim.x) {
@@ -258,6 +266,7 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
         edgePass<A>(I, I.x, false);
         __syncthreads();
       }
+      clk.lap(I, threadIdx.x == 0, kStageUnpack);  // the residual scan and the gate belong to the convergence scan
       diff = blockMax(diff, red);
       // gate (Integrator.cpp:676-747)
       if (threadIdx.x == 0) {
@@ -295,6 +304,8 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
       if (conv) *I.earlyExits += 1;
     }
     __syncthreads();
+    clk.lap(I, threadIdx.x == 0, kStageVelocity);
+    clk.finish(I, threadIdx.x == 0);
   }
 }
 

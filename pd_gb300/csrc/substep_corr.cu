@@ -196,6 +196,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
   tm.sync();
 
   const int gl = TID & (kLanesPerVertex - 1), group = TID / kLanesPerVertex, ngroups = NT / kLanesPerVertex;
+  const StageClock clk(I, TID == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict (Integrator.cpp:447-472): x_n in FP64, x̂ as a pair
     double sc = 0.0;
@@ -211,6 +212,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       sc = fmax(sc, fabs(xh - p));
     }
     const double scMax = teamMax(tm, sc, red, slots, parity);
+    clk.lap(I, TID == 0, kStagePredict);
     const double scale = (scMax < I.gScaleHH) ? I.gScaleHH : scMax;
     int used = 0;
     bool conv = false;
@@ -251,6 +253,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       // correction and residual of x^k; the residual gates iteration k − 1 unless that iteration
       // was over-relaxed and gated on its own solve's residual below
       const double resMax = correctionPass(true);
+      clk.lap(I, TID == 0, kStageLocal);
       bool stop = k == I.maxIter;
       if (I.useResidual && k >= 1 && k - 1 < I.chebFrom) {
         lastRes = resMax;
@@ -261,6 +264,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       }
       if (stop) break;
       TeamSolve32<CLUSTER>::run(I, tm, Y, T);  // Y ← Δ
+      clk.lap(I, TID == 0, kStageSolve);
       // x^{k+1} = x^k + Δ as pairs; pinned rows take q. An over-relaxed iteration
       // (Integrator.cpp:631-641) puts x^k + ω·Δ; with the residual gate it first puts x^k + Δ,
       // takes that point's residual, then adds (ω − 1)·Δ.
@@ -300,6 +304,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
           xf[8 * v + 4 + c] = lo;
         }
         tm.sync();
+        clk.lap(I, TID == 0, kStageUnpack);
         lastRes = resSolve;
         used = k + 1;
         if (I.resTrace && TID == 0) I.resTrace[(size_t)step * I.maxIter + k] = resSolve;
@@ -308,6 +313,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
         continue;
       }
       const double diff = teamMax(tm, dmax, red, slots, parity);
+      clk.lap(I, TID == 0, kStageUnpack);
       if (!I.useResidual) {
         const double rel = (scale > 0.0) ? diff / scale : diff;
         const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
@@ -341,6 +347,8 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
       if (conv) *I.earlyExits += 1;
     }
     tm.sync();
+    clk.lap(I, TID == 0, kStageVelocity);
+    clk.finish(I, TID == 0);
   }
   for (int t = TID; t < n3; t += NT) {
     const int v = t / 3, c = t - 3 * v;

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   const int q4 = ld / 4;
   __syncthreads();
 
+  const StageClock clk(I, rank == 0 && threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict own rows (Integrator.cpp:447-472), x̂ kept as a hi/lo pair
     double sc = 0.0;
@@ -282,6 +283,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     }
     const float scW = static_cast<float>(warpMaxD(sc));
     __syncthreads();  // x̂ of own rows is read by other threads below
+    clk.lap(I, rank == 0 && threadIdx.x == 0, kStagePredict);
     double scale = 0.0;
     int used = 0;
     bool conv = false;
@@ -332,6 +334,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       resLocal = warpMaxF(resLocal);
       if (lane == 0) red[warp] = (k == 0) ? scW : resLocal;
       __syncthreads();
+      clk.lap(I, rank == 0 && threadIdx.x == 0, kStageLocal);  // the correction pass: projection, scatter and residual in one
       bool ok = true;
       if (warp == 0) {
         if (lane == 0) {
@@ -379,6 +382,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         }
       }
       __syncthreads();
+      clk.lap(I, rank == 0 && threadIdx.x == 0, kStageSolve);  // exchange A (the whole correction) and this CTA's rows of Ã⁻¹·r
       // x^{k+1} = x^k + Δ as hi/lo pairs (pinned rows: q), published for the team
       const unsigned tagB = ++epoch;
       float dmax = 0.f;
@@ -433,6 +437,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
+      clk.lap(I, rank == 0 && threadIdx.x == 0, kStageUnpack);  // the two-sum update and exchange B (the window's positions)
       if (split) {
         // residual of x^k + Δ for own vertices, sent with the next exchange A
         resSplit = 0.f;
@@ -502,6 +507,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (conv) *I.earlyExits += 1;
     }
     __syncthreads();
+    clk.lap(I, rank == 0 && threadIdx.x == 0, kStageVelocity);
+    clk.finish(I, rank == 0 && threadIdx.x == 0);
   }
   if (rank == 0 && threadIdx.x == 0) *I.epoch = epoch;
   for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {

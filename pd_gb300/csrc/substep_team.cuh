@@ -345,6 +345,7 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
                                 double* red, double* slots) {
   int parity = 0;
   const int T = tm.tid(), NT = tm.count();
+  const StageClock clk(I, tm.rank == 0 && threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     double scale = 0.0;
     for (int v = T; v < I.n; v += NT) {  // predict (Integrator.cpp:447-472)
@@ -361,16 +362,20 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
       scale = fmax(scale, maxAbs3(d[0], d[1], d[2]));
     }
     scale = teamMax(tm, scale, red, slots, parity);
+    clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStagePredict);
     scale = (scale < I.gScaleHH) ? I.gScaleHH : scale;
     for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, I.x, e, false);  // projection of x_n
     tm.sync();
+    clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageLocal);
     int used = 0;
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
     for (int k = 0; k < I.maxIter; ++k) {
       for (int v = T; v < I.n; v += NT) gatherRow(I, tm, v, w);
       tm.sync();
+      clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageScatter);
       TeamSolve<CLUSTER>::run(I, tm, w, t);
+      clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageSolve);
       // unpack + displacement scan; an over-relaxed iteration puts x_prev + (x_solve − x_prev)·ω
       // and keeps x_solve for the residual (Integrator.cpp:631-641)
       const bool blend = k >= I.chebFrom;
@@ -391,9 +396,11 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
         }
       }
       tm.sync();
+      clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageUnpack);
       const double* X = split ? I.xsol : I.x;
       for (int e = T; e < I.ne; e += NT) edgeTerms(I, tm, X, e, I.useResidual != 0);
       tm.sync();
+      clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageLocal);
       double res = 0.0;
       if (I.useResidual) {
         for (int v = T; v < I.n; v += NT) {
@@ -408,6 +415,7 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
         tm.sync();
       }
       diff = teamMax(tm, diff, red, slots, parity);
+      clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageUnpack);
       // gate (Integrator.cpp:676-747): every thread holds the reduced values and decides alike
       const double rel = (scale > 0.0) ? diff / scale : diff;
       const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
@@ -437,6 +445,8 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
       if (conv) *I.earlyExits += 1;
     }
     tm.sync();
+    clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageVelocity);
+    clk.finish(I, tm.rank == 0 && threadIdx.x == 0);
   }
 }
 
