@@ -263,7 +263,8 @@ int pd_sim_step_host(pd_sim* s, int32_t substeps);
  * correction and its rows of Ã⁻¹); unpack_scan (unpack, the displacement / residual scan and the
  * gate; the team kernel's update and position exchange); velocity. `assemble` is host wall time
  * of the (re)factorizations of this instance, device refactorizations and re-uploads included.
- * Timing slows nothing measurable: one thread reads a clock a few times per iteration. */
+ * While timing is on the kernels run as separately compiled timed variants (the untimed ones carry
+ * no timing code); the FP32_SOLVE kernels are not timed (their device stages stay 0). */
 typedef struct pd_stage_times {
   double predict, local_step, scatter, assemble, solve, unpack_scan, velocity, total;
 } pd_stage_times;

@@ -1055,14 +1055,14 @@ struct pd_sim {
     int rc;
     const int p = precision();
     if (p == PD_PRECISION_FP64_EXACT) {
-      rc = pdg::launchSubstepExact(dDesc, count, substeps, smemBytes, st);
+      rc = pdg::launchSubstepExact(dDesc, count, substeps, smemBytes, st, stageTiming);
     } else if (delta) {
-      rc = pdg::launchSubstepDelta(dDesc, count, teamCtas, smemBytes, substeps, st);
+      rc = pdg::launchSubstepDelta(dDesc, count, teamCtas, smemBytes, substeps, st, stageTiming);
     } else if (corr) {
       if (teamCtas > 16) {  // one cloth on a cooperative grid of CTAs
-        rc = pdg::launchSubstepCorrGrid(dDesc, teamCtas, substeps, st);
+        rc = pdg::launchSubstepCorrGrid(dDesc, teamCtas, substeps, st, stageTiming);
       } else if (teamCtas > 1) {
-        rc = pdg::launchSubstepCorrCluster(dDesc, count, teamCtas, substeps, st);
+        rc = pdg::launchSubstepCorrCluster(dDesc, count, teamCtas, substeps, st, stageTiming);
       } else if (corrBig > 0) {
         // the one-CTA launch of the smaller cloths on this stream, submitted first, then the large
         // cloths' clusters on the second stream behind an event wait: the one-CTA cloths take
@@ -1070,17 +1070,17 @@ struct pd_sim {
         // clusters dispatched first the batch needs more than one wave of them before the rest
         // start (512-cloth batch: 35.0 against 29.4 ms per substep).
         PD_CUDA(cudaEventRecord(forkEv, st));
-        rc = pdg::launchSubstepCorr(dDescOrder + corrBig, count - corrBig, substeps, smemBytes, st);
+        rc = pdg::launchSubstepCorr(dDescOrder + corrBig, count - corrBig, substeps, smemBytes, st, stageTiming);
         if (rc == 0) {
           PD_CUDA(cudaStreamWaitEvent(aux, forkEv, 0));
-          rc = pdg::launchSubstepCorrCluster(dDescOrder, corrBig, bigCs, substeps, aux);
+          rc = pdg::launchSubstepCorrCluster(dDescOrder, corrBig, bigCs, substeps, aux, stageTiming);
         }
         if (rc == 0) {
           PD_CUDA(cudaEventRecord(joinEv, aux));
           PD_CUDA(cudaStreamWaitEvent(st, joinEv, 0));
         }
       } else {
-        rc = pdg::launchSubstepCorr(dDescOrder ? dDescOrder : dDesc, count, substeps, smemBytes, st);
+        rc = pdg::launchSubstepCorr(dDescOrder ? dDescOrder : dDesc, count, substeps, smemBytes, st, stageTiming);
       }
     } else if (dense) {
       rc = pdg::launchSubstepDenseCluster(dDesc, count, teamCtas, smemBytes, substeps, st);
@@ -1088,9 +1088,9 @@ struct pd_sim {
       rc = teamCtas > 1 ? pdg::launchSubstepMixedCluster(dDesc, count, teamCtas, smemBytes, substeps, st)
                         : pdg::launchSubstepMixed(dDesc, count, substeps, smemBytes, st);
     } else {
-      rc = teamCtas > 16  ? pdg::launchSubstepGrid(dDesc, teamCtas, substeps, st)
-           : teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st)
-                          : pdg::launchSubstepFast(dDesc, count, substeps, smemBytes, st);
+      rc = teamCtas > 16  ? pdg::launchSubstepGrid(dDesc, teamCtas, substeps, st, stageTiming)
+           : teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st, stageTiming)
+                          : pdg::launchSubstepFast(dDesc, count, substeps, smemBytes, st, stageTiming);
     }
     if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "substep launch");
     return PD_OK;

@@ -144,7 +144,17 @@ enum StageIndex { kStagePredict = 0, kStageLocal, kStageScatter, kStageSolve, kS
 static __shared__ unsigned long long stageStamp[2];  // start of the substep, last lap
 static __shared__ int stageOn;                        // this CTA times stages (rank 0, stageNs set)
 
+// TIMED = false (every launch unless stage timing is on): no code at all, so the untimed kernels
+// are compiled exactly as without timing; the timed instantiations are launched only while it is on.
+template <bool TIMED>
 struct StageClock {
+  __device__ __forceinline__ StageClock(const InstanceDev&, bool) {}
+  __device__ __forceinline__ void lap(const InstanceDev&, bool, int) const {}
+  __device__ __forceinline__ void finish(const InstanceDev&, bool) const {}
+};
+
+template <>
+struct StageClock<true> {
   __device__ __forceinline__ StageClock(const InstanceDev& I, bool thread0) {
     if (thread0) {
       stageOn = I.stageNs != nullptr;
@@ -173,20 +183,22 @@ struct StageClock {
 
 // Launch the reference-order FP64 substep kernel over `count` instances.
 int launchSubstepExact(const InstanceDev* dInstances, int count, int substeps, int smemBytes,
-                       void* stream);
+                       void* stream, bool timed = false);
 // Reference-order FP64 3-column solve for one instance: b (3n, vertex order) → x.
 int launchSolveExact(const InstanceDev* dInstance, const double* b, double* x, int smemBytes,
                      void* stream);
 // FP64 substep with the supernodal solve (smem: 6n doubles when they fit).
-int launchSubstepFast(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
+int launchSubstepFast(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream,
+                      bool timed = false);
 int launchSolveFast(const InstanceDev* dInstance, const double* b, double* x, int smemBytes, void* stream);
 // FP64 supernodal substep with `clusterSize` CTAs (a thread-block cluster) per instance.
-int launchSubstepCluster(const InstanceDev* dInstances, int count, int clusterSize, int substeps, void* stream);
+int launchSubstepCluster(const InstanceDev* dInstances, int count, int clusterSize, int substeps, void* stream,
+                         bool timed = false);
 // `want` if a cluster of that many 256-thread CTAs can run on this device, else 0.
 int clusterSizeSupported(int want);
 // One cloth (dInstances[0]) of the FP64 supernodal substep by `ctas` co-resident CTAs on a
 // cooperative launch (the cluster code with grid barriers); gridCapacity: the most CTAs it holds.
-int launchSubstepGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream);
+int launchSubstepGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
 int gridCapacity();
 // Mixed-precision substep (FP32 solve + one FP64 refinement step): one CTA per instance with
 // smemBytes of workspace (72·n when it fits, else 0 = global), or a cluster of clusterSize CTAs
@@ -202,19 +214,22 @@ int launchSubstepDenseCluster(const InstanceDev* dInstances, int count, int clus
 int denseClusterSupported(int clusterSize, int smemBytes);
 // MIXED substep for small cloths by `team` co-resident CTAs per instance (cooperative launch):
 // x ← x + Ã⁻¹·(b − Ã·x) with the rows of the explicit FP32 inverse split over the team.
-int launchSubstepDelta(const InstanceDev* dInstances, int count, int team, int smemBytes, int substeps, void* stream);
+int launchSubstepDelta(const InstanceDev* dInstances, int count, int team, int smemBytes, int substeps, void* stream,
+                       bool timed = false);
 // CTAs of kDeltaThreads threads with smemBytes each that can be co-resident on the device.
 int deltaResidentCtas(int smemBytes);
 // MIXED substep for cloths above the explicit-inverse limit, one CTA per instance: x ← x +
 // L⁻¹·(b − Ã·x) with the FP32 supernodal solve (smemBytes: 24·n when the solve vectors fit).
-int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream);
+int launchSubstepCorr(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream,
+                      bool timed = false);
 // The same by a thread-block cluster of `cs` 256-thread CTAs per instance (vectors in L2).
-int launchSubstepCorrCluster(const InstanceDev* dInstances, int count, int cs, int substeps, void* stream);
+int launchSubstepCorrCluster(const InstanceDev* dInstances, int count, int cs, int substeps, void* stream,
+                             bool timed = false);
 // `cs` if a cluster of that many correction-kernel CTAs can run on this device, else 0.
 int corrClusterSupported(int cs);
 // One cloth (dInstances[0]) by `ctas` co-resident CTAs on a cooperative launch: the cluster code
 // with grid barriers. corrGridCapacity: the most CTAs such a launch can hold on this device.
-int launchSubstepCorrGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream);
+int launchSubstepCorrGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
 int corrGridCapacity();
 constexpr int kDeltaThreads = 512;
 

@@ -183,9 +183,9 @@ __device__ double vertexResidual(const InstanceDev& I, const double* X, int v) {
 
 // Whole substeps of one instance. `w` holds the RHS / solution in elimination order; the
 // solver may use `t` as a second workspace of the same size.
-template <class A, class Solve>
+template <class A, class Solve, bool TIMED = false>
 __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, double* t, double* red, int* flag) {
-  const StageClock clk(I, threadIdx.x == 0);
+  const StageClock<TIMED> clk(I, threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict x̂ = x + h·v + h²·g, x_n = x, bBase = (M/h²)·x̂ (Integrator.cpp:447-472); the
     // displacement scale max|x̂ − x_n|∞ is the same in every iteration of the substep.
@@ -218,7 +218,7 @@ __device__ void runSubsteps(const InstanceDev& I, int substeps, double* w, doubl
       __syncthreads();
       clk.lap(I, threadIdx.x == 0, kStageScatter);
       Solve::run(I, w, t);
-      __syncthreads();
+      if (TIMED) __syncthreads();
       clk.lap(I, threadIdx.x == 0, kStageSolve);
       // unpack + displacement scan (Integrator.cpp:618-663); an over-relaxed iteration puts
       // x_prev + (x_solve − x_prev)·ω and keeps x_solve for the residual (:631-641)

@@ -15,6 +15,8 @@
 // are separated by cluster barriers, data other CTAs write are read through L2, and reductions go
 // through distributed shared memory. Positions and x̂ (as pairs) and the solve's two vectors live
 // in the instance's arrays; a one-CTA cloth keeps the solve vectors in shared memory when they fit.
+#include <algorithm>
+
 #include "correction.cuh"
 #include "solve32.cuh"
 #include "substep_team.cuh"
@@ -173,7 +175,7 @@ struct TeamSolve32 {
   }
 };
 
-template <bool CLUSTER>
+template <bool CLUSTER, bool TIMED = false>
 __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, int substeps, float* Y, float* T,
                                 double* red, double* slots) {
   int parity = 0;
@@ -196,7 +198,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
   tm.sync();
 
   const int gl = TID & (kLanesPerVertex - 1), group = TID / kLanesPerVertex, ngroups = NT / kLanesPerVertex;
-  const StageClock clk(I, TID == 0);
+  const StageClock<TIMED> clk(I, TID == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict (Integrator.cpp:447-472): x_n in FP64, x̂ as a pair
     double sc = 0.0;
@@ -357,6 +359,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
   }
 }
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const InstanceDev* __restrict__ insts,
                                                                      int substeps, int smemBytes) {
   extern __shared__ float sm[];
@@ -367,9 +370,10 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
   float* Y = inSmem ? sm : I.y32;
   float* T = inSmem ? sm + 3 * I.n : I.t32;
   const Team<false> tm{0, 1};
-  runSubstepsCorr<false>(I, tm, substeps, Y, T, red, slots);
+  runSubstepsCorr<false, TIMED>(I, tm, substeps, Y, T, red, slots);
 }
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const InstanceDev* __restrict__ insts,
                                                                          int substeps) {
   __shared__ double red[32];
@@ -378,12 +382,13 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const 
   const int cs = static_cast<int>(cl.num_blocks());
   const InstanceDev& I = insts[blockIdx.x / cs];
   const Team<true> tm{static_cast<int>(cl.block_rank()), cs};
-  runSubstepsCorr<true>(I, tm, substeps, I.y32, I.t32, red, slots);
+  runSubstepsCorr<true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
 // One large cloth on a cooperative grid of CTAs (more SMs than a cluster holds): the cluster code
 // path with grid barriers; the instance's FP64 solve workspace (unused by the correction kernels)
 // holds the per-CTA slots of the team maxima.
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepCorrGridKernel(const InstanceDev* __restrict__ insts,
                                                                       int substeps) {
   __shared__ double red[32];
@@ -391,7 +396,7 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrGridKernel(const Ins
   const InstanceDev& I = insts[0];
   Team<true> tm{static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x)};
   tm.gslots = I.w;
-  runSubstepsCorr<true>(I, tm, substeps, I.y32, I.t32, red, slots);
+  runSubstepsCorr<true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
 cudaLaunchConfig_t corrClusterConfig(int blocks, int cs, void* stream, cudaLaunchAttribute* attr) {
@@ -411,42 +416,55 @@ cudaLaunchConfig_t corrClusterConfig(int blocks, int cs, void* stream, cudaLaunc
 
 }  // namespace
 
-int launchSubstepCorr(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream) {
+int launchSubstepCorr(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream, bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   static bool attrSet = false;
   if (!attrSet) {
-    cudaFuncSetAttribute(substepCorrKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepCorrKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepCorrKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attrSet = true;
   }
-  substepCorrKernel<<<count, kBlockThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(d, substeps, smemBytes);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (timed) substepCorrKernel<true><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
+  else substepCorrKernel<false><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
 }
 
 int corrClusterSupported(int cs) {
   if (cs < 2 || cs > 16) return 0;
-  if (cs > 8) cudaFuncSetAttribute(substepCorrClusterKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = corrClusterConfig(cs, cs, nullptr, attr);
-  int clusters = 0;
-  const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, substepCorrClusterKernel, &cfg);
-  if (e != cudaSuccess) cudaGetLastError();
-  return (e == cudaSuccess && clusters > 0) ? cs : 0;
+  for (auto kernel : {substepCorrClusterKernel<false>, substepCorrClusterKernel<true>}) {  // both must run
+    if (cs > 8) cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = corrClusterConfig(cs, cs, nullptr, attr);
+    int clusters = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg);
+    if (e != cudaSuccess) cudaGetLastError();
+    if (e != cudaSuccess || clusters <= 0) return 0;
+  }
+  return cs;
 }
 
 int corrGridCapacity() {
   static int cached = -1;
   if (cached >= 0) return cached;
-  int dev = 0, sms = 0, perSm = 0;
+  int dev = 0, sms = 0, least = 1 << 30;
   cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepCorrGridKernel, kBlockThreads, 0) != cudaSuccess) {
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
     cudaGetLastError();
     return cached = 0;
   }
-  return cached = perSm * sms;
+  for (auto kernel : {substepCorrGridKernel<false>, substepCorrGridKernel<true>}) {  // both must fit
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kBlockThreads, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return cached = 0;
+    }
+    least = std::min(least, perSm);
+  }
+  return cached = least * sms;
 }
 
-int launchSubstepCorrGrid(const InstanceDev* d, int ctas, int substeps, void* stream) {
+int launchSubstepCorrGrid(const InstanceDev* d, int ctas, int substeps, void* stream, bool timed) {
   if (substeps <= 0) return 0;
   if (ctas < 2 || ctas > corrGridCapacity()) return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
   cudaLaunchConfig_t cfg = {};
@@ -458,16 +476,18 @@ int launchSubstepCorrGrid(const InstanceDev* d, int ctas, int substeps, void* st
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepCorrGridKernel, d, substeps);
+  const cudaError_t e = timed ? cudaLaunchKernelEx(&cfg, substepCorrGridKernel<true>, d, substeps)
+                              : cudaLaunchKernelEx(&cfg, substepCorrGridKernel<false>, d, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 
-int launchSubstepCorrCluster(const InstanceDev* d, int count, int cs, int substeps, void* stream) {
+int launchSubstepCorrCluster(const InstanceDev* d, int count, int cs, int substeps, void* stream, bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   if (corrClusterSupported(cs) != cs) return static_cast<int>(cudaErrorInvalidConfiguration);
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = corrClusterConfig(count * cs, cs, stream, attr);
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepCorrClusterKernel, d, substeps);
+  const cudaError_t e = timed ? cudaLaunchKernelEx(&cfg, substepCorrClusterKernel<true>, d, substeps)
+                              : cudaLaunchKernelEx(&cfg, substepCorrClusterKernel<false>, d, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 

@@ -35,6 +35,8 @@
 // poll gives up after a bounded number of rounds, setting the instance's error flag.
 #include <cstdint>
 
+#include <algorithm>
+
 #include "correction.cuh"
 #include "device.cuh"
 
@@ -195,6 +197,7 @@ __device__ __forceinline__ void rowGroup(const float* A0, int nr, const float* R
         for (int c = 0; c < 3; ++c) dl[3 * (li + r) + c] = s[r][c];
 }
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const InstanceDev* __restrict__ insts,
                                                                       int team, int substeps) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   const int q4 = ld / 4;
   __syncthreads();
 
-  const StageClock clk(I, rank == 0 && threadIdx.x == 0);
+  const StageClock<TIMED> clk(I, rank == 0 && threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict own rows (Integrator.cpp:447-472), x̂ kept as a hi/lo pair
     double sc = 0.0;
@@ -525,19 +528,24 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
 int deltaResidentCtas(int smemBytes) {
   constexpr int kMaxDynamic = 224 * 1024;  // leaves room for the kernel's static shared memory
   if (smemBytes > kMaxDynamic) return 0;
-  cudaFuncSetAttribute(substepDeltaKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynamic);
-  int perSm = 0, dev = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepDeltaKernel, kDeltaThreads, smemBytes) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return 0;
+  int least = 1 << 30;
+  for (auto kernel : {substepDeltaKernel<false>, substepDeltaKernel<true>}) {  // both must fit
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynamic);
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kDeltaThreads, smemBytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    least = std::min(least, perSm);
   }
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return perSm * sms;
+  return least * sms;
 }
 
-int launchSubstepDelta(const InstanceDev* d, int count, int team, int smemBytes, int substeps, void* stream) {
+int launchSubstepDelta(const InstanceDev* d, int count, int team, int smemBytes, int substeps, void* stream,
+                       bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   if (team > kMaxTeam || deltaResidentCtas(smemBytes) < count * team)
     return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
@@ -551,7 +559,8 @@ int launchSubstepDelta(const InstanceDev* d, int count, int team, int smemBytes,
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepDeltaKernel, d, team, substeps);
+  const cudaError_t e = timed ? cudaLaunchKernelEx(&cfg, substepDeltaKernel<true>, d, team, substeps)
+                              : cudaLaunchKernelEx(&cfg, substepDeltaKernel<false>, d, team, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 

@@ -53,6 +53,7 @@ struct ExactSolve {
   }
 };
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepExactKernel(const InstanceDev* __restrict__ insts,
                                                                     int substeps, int smemBytes) {
   extern __shared__ double smem[];
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(kBlockThreads) substepExactKernel(const Instan
   __shared__ int flag;
   const InstanceDev& I = insts[blockIdx.x];
   double* w = (3 * I.n * (int)sizeof(double) <= smemBytes) ? smem : I.w;
-  runSubsteps<ExactArith, ExactSolve>(I, substeps, w, nullptr, red, &flag);
+  runSubsteps<ExactArith, ExactSolve, TIMED>(I, substeps, w, nullptr, red, &flag);
 }
 
 __global__ void __launch_bounds__(kBlockThreads) solveExactKernel(const InstanceDev* __restrict__ inst,
@@ -87,14 +88,17 @@ __global__ void __launch_bounds__(kBlockThreads) solveExactKernel(const Instance
 
 }  // namespace
 
-int launchSubstepExact(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream) {
+int launchSubstepExact(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream, bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   static bool attrSet = false;
   if (!attrSet) {
-    cudaFuncSetAttribute(substepExactKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepExactKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepExactKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attrSet = true;
   }
-  substepExactKernel<<<count, kBlockThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(d, substeps, smemBytes);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (timed) substepExactKernel<true><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
+  else substepExactKernel<false><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
 }
 

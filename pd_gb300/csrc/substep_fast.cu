@@ -16,6 +16,7 @@
 namespace pdg {
 namespace {
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepFastKernel(const InstanceDev* __restrict__ insts,
                                                                    int substeps, int smemBytes) {
   extern __shared__ double smem[];
@@ -26,9 +27,10 @@ __global__ void __launch_bounds__(kBlockThreads) substepFastKernel(const Instanc
   double* w = inSmem ? smem : I.w;
   double* t = inSmem ? smem + 3 * I.n : I.tbuf;
   const Team<false> tm{0, 1};
-  runSubstepsTeam<false>(I, tm, substeps, w, t, red, slots);
+  runSubstepsTeam<false, TIMED>(I, tm, substeps, w, t, red, slots);
 }
 
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepClusterKernel(const InstanceDev* __restrict__ insts,
                                                                       int substeps) {
   __shared__ double red[32];
@@ -37,11 +39,12 @@ __global__ void __launch_bounds__(kBlockThreads) substepClusterKernel(const Inst
   const int cs = static_cast<int>(cl.num_blocks());
   const InstanceDev& I = insts[blockIdx.x / cs];
   const Team<true> tm{static_cast<int>(cl.block_rank()), cs};
-  runSubstepsTeam<true>(I, tm, substeps, I.w, I.tbuf, red, slots);
+  runSubstepsTeam<true, TIMED>(I, tm, substeps, I.w, I.tbuf, red, slots);
 }
 
 // One large cloth on a cooperative grid of CTAs: the cluster code with grid barriers; the
 // instance's FP64 refinement workspace x0 (unused in the FP64 modes) holds the team-maximum slots.
+template <bool TIMED>
 __global__ void __launch_bounds__(kBlockThreads) substepGridKernel(const InstanceDev* __restrict__ insts,
                                                                    int substeps) {
   __shared__ double red[32];
@@ -49,7 +52,7 @@ __global__ void __launch_bounds__(kBlockThreads) substepGridKernel(const Instanc
   const InstanceDev& I = insts[0];
   Team<true> tm{static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x)};
   tm.gslots = I.x0;
-  runSubstepsTeam<true>(I, tm, substeps, I.w, I.tbuf, red, slots);
+  runSubstepsTeam<true, TIMED>(I, tm, substeps, I.w, I.tbuf, red, slots);
 }
 
 __global__ void __launch_bounds__(kBlockThreads) solveFastKernel(const InstanceDev* __restrict__ inst,
@@ -116,14 +119,17 @@ cudaLaunchConfig_t clusterConfig(int blocks, int clusterSize, int smemBytes, voi
 
 }  // namespace
 
-int launchSubstepFast(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream) {
+int launchSubstepFast(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream, bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   static bool attrSet = false;
   if (!attrSet) {
-    cudaFuncSetAttribute(substepFastKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepFastKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepFastKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attrSet = true;
   }
-  substepFastKernel<<<count, kBlockThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(d, substeps, smemBytes);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (timed) substepFastKernel<true><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
+  else substepFastKernel<false><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -131,30 +137,41 @@ int clusterSizeSupported(int want) {
   static int cached[17] = {0};
   if (want < 1 || want > 16) return 0;
   if (cached[want]) return cached[want] > 0 ? want : 0;
-  if (want > 8) cudaFuncSetAttribute(substepClusterKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = clusterConfig(want, want, 0, nullptr, attr);
-  int clusters = 0;
-  const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, substepClusterKernel, &cfg);
-  if (e != cudaSuccess) cudaGetLastError();
-  cached[want] = (e == cudaSuccess && clusters > 0) ? 1 : -1;
-  return cached[want] > 0 ? want : 0;
+  bool ok = true;
+  for (auto kernel : {substepClusterKernel<false>, substepClusterKernel<true>}) {  // both must run
+    if (want > 8) cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = clusterConfig(want, want, 0, nullptr, attr);
+    int clusters = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg);
+    if (e != cudaSuccess) cudaGetLastError();
+    ok = ok && e == cudaSuccess && clusters > 0;
+  }
+  cached[want] = ok ? 1 : -1;
+  return ok ? want : 0;
 }
 
 int gridCapacity() {
   static int cached = -1;
   if (cached >= 0) return cached;
-  int dev = 0, sms = 0, perSm = 0;
+  int dev = 0, sms = 0, least = 1 << 30;
   cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepGridKernel, kBlockThreads, 0) != cudaSuccess) {
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
     cudaGetLastError();
     return cached = 0;
   }
-  return cached = perSm * sms;
+  for (auto kernel : {substepGridKernel<false>, substepGridKernel<true>}) {  // both must fit
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kBlockThreads, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return cached = 0;
+    }
+    least = least < perSm ? least : perSm;
+  }
+  return cached = least * sms;
 }
 
-int launchSubstepGrid(const InstanceDev* d, int ctas, int substeps, void* stream) {
+int launchSubstepGrid(const InstanceDev* d, int ctas, int substeps, void* stream, bool timed) {
   if (substeps <= 0) return 0;
   if (ctas < 2 || ctas > gridCapacity()) return static_cast<int>(cudaErrorCooperativeLaunchTooLarge);
   cudaLaunchConfig_t cfg = {};
@@ -166,16 +183,18 @@ int launchSubstepGrid(const InstanceDev* d, int ctas, int substeps, void* stream
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepGridKernel, d, substeps);
+  const cudaError_t e = timed ? cudaLaunchKernelEx(&cfg, substepGridKernel<true>, d, substeps)
+                              : cudaLaunchKernelEx(&cfg, substepGridKernel<false>, d, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 
-int launchSubstepCluster(const InstanceDev* d, int count, int clusterSize, int substeps, void* stream) {
+int launchSubstepCluster(const InstanceDev* d, int count, int clusterSize, int substeps, void* stream, bool timed) {
   if (count <= 0 || substeps <= 0) return 0;
   if (clusterSizeSupported(clusterSize) != clusterSize) return static_cast<int>(cudaErrorInvalidConfiguration);
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = clusterConfig(count * clusterSize, clusterSize, 0, stream, attr);
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, substepClusterKernel, d, substeps);
+  const cudaError_t e = timed ? cudaLaunchKernelEx(&cfg, substepClusterKernel<true>, d, substeps)
+                              : cudaLaunchKernelEx(&cfg, substepClusterKernel<false>, d, substeps);
   return static_cast<int>(e != cudaSuccess ? e : cudaGetLastError());
 }
 

@@ -340,12 +340,12 @@ struct TeamSolve {
 
 // Whole substeps of one instance by a team (same steps and formulas as runSubsteps in
 // substep_common.cuh, with FMA contraction allowed).
-template <bool CLUSTER>
+template <bool CLUSTER, bool TIMED = false>
 __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, int substeps, double* w, double* t,
                                 double* red, double* slots) {
   int parity = 0;
   const int T = tm.tid(), NT = tm.count();
-  const StageClock clk(I, tm.rank == 0 && threadIdx.x == 0);
+  const StageClock<TIMED> clk(I, tm.rank == 0 && threadIdx.x == 0);
   for (int step = 0; step < substeps; ++step) {
     double scale = 0.0;
     for (int v = T; v < I.n; v += NT) {  // predict (Integrator.cpp:447-472)
