@@ -837,7 +837,20 @@ struct pd_sim {
     if (rc != PD_OK) return rc;
     for (auto& I : inst)  // numeric refactorizations on the device, before anything reads the factor
       if (I.gpuRefactor)
-        if (const int rc2 = refactorOnDevice(I)) return rc2;
+        if (const int rc2 = refactorOnDevice(I)) {
+          // the device factor is partly overwritten: lay the previous host factor out again, as a
+          // failed host factorization leaves it, and let the next stamp change refactorize
+          const std::string msg = g_lastError;
+          for (auto& J : inst)
+            if (J.gpuRefactor) {
+              J.gpuRefactor = false;
+              J.factorizeCount -= 1;
+              J.stamp = pdg::Stamp{};
+            }
+          upload(capacity);
+          g_lastError = msg;
+          return rc2;
+        }
     for (size_t i = 0; i < inst.size(); ++i) {  // explicit inverses from the uploaded FP64 factors
       if (inst[i].denseLd <= 0) continue;
       const int e = pdg::launchDenseInverse(dDesc + i, inst[i].scene.n, stream);
@@ -1980,7 +1993,12 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (rc != PD_OK) return rc;
+  if (rc != PD_OK) {  // back to the plan and state the handle had (best effort), then report
+    const std::string msg = g_lastError;
+    if (replan(s, start, o, s->logCapacity > 0 ? s->logCapacity : 1) == PD_OK) restoreCounters(s, o);
+    g_lastError = msg;
+    return rc;
+  }
   const size_t b = best();
   if (const int rc2 = replan(s, plans[b], o, s->logCapacity > 0 ? s->logCapacity : 1)) return rc2;
   if (const int rc2 = restoreCounters(s, o)) return rc2;
