@@ -5,6 +5,13 @@ The compute path is the in-tree CUDA library ``pd_gb300/_lib/libpd_gb300.so`` (b
 bindings raises if the library is missing.
 """
 from .api import (  # noqa: F401
+    PD_OK,
+    PD_ERR_INVALID_ARGUMENT,
+    PD_ERR_STATE,
+    PD_ERR_FACTORIZATION,
+    PD_ERR_CUDA,
+    PD_ERR_UNSUPPORTED,
+    PD_ERR_NO_MEMORY,
     PD_PRECISION_FP64_EXACT,
     PD_PRECISION_FP64,
     PD_PRECISION_FP32_PROJECTION,

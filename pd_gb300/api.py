@@ -16,6 +16,12 @@ from dataclasses import dataclass, field, fields
 import numpy as np
 
 PD_OK = 0
+PD_ERR_INVALID_ARGUMENT = 1       # PdError.code values (PD_ERR_* in include/pd_gb300.h)
+PD_ERR_STATE = 2
+PD_ERR_FACTORIZATION = 3
+PD_ERR_CUDA = 4
+PD_ERR_UNSUPPORTED = 5
+PD_ERR_NO_MEMORY = 6
 PD_PRECISION_FP64_EXACT = 0       # FP64 in the reference's operation order (bit-identical)
 PD_PRECISION_FP64 = 1             # FP64, supernodal solve (matches to rounding)
 PD_PRECISION_FP32_PROJECTION = 2  # FP32 projection, FP64 supernodal solve

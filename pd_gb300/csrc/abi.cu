@@ -150,7 +150,12 @@ std::string prepare(Instance& I, bool reanalyze) {
     pdg::refreshAval(I.F, I.L);
     I.gpuRefactor = true;
   } else {
-    if (!pdg::factorize(I.L, perm, I.F, &err)) return err;
+    pdg::Factor fresh;  // a failed factorization leaves the previous factor whole
+    if (!pdg::factorize(I.L, perm, fresh, &err)) {
+      I.stamp = pdg::Stamp{};  // L holds the failed values: the next edit rebuilds from the scene
+      return err;
+    }
+    I.F = std::move(fresh);
     pdg::buildSupernodal(I.F, I.tree);
     pdg::buildMixed(I.F, I.L);
     if (c.precision != PD_PRECISION_FP64_EXACT) pdg::buildRefactorMaps(I.F);

@@ -107,3 +107,30 @@ def test_reference_order_and_forced_host_path(pdg, monkeypatch):
     sim1 = pdg.Simulator(scene, cfg1)
     sim1.set_edge_stiffness(k2)
     assert sim1.info()["device_factorize_count"] == 0 and sim1.info()["factorize_count"] == 2
+
+
+@pytest.mark.parametrize("p", [0, 1, 4])
+def test_failed_refactorization_keeps_the_handle(pdg, p):
+    """A stiffness change whose Ã has a non-finite pivot (one edge of infinite stiffness) fails with
+    PD_ERR_FACTORIZATION on the host path (reference order) and on the device path (the others);
+    the handle keeps a whole factor, and after the stiffness is put back it steps like the oracle
+    that never saw the change."""
+    cfg = cfg_with(W._base(grid_nx=14, grid_ny=12, grid_spacing=1 / 13, max_iterations=8, shear_stiffness=700.0), p)
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    sim.step(3)
+    orc.step(3)
+    k = np.asarray(scene.edge_stiffness, np.float64).copy()
+    bad = k.copy()
+    bad[len(bad) // 2] = np.inf
+    with pytest.raises(pdg.PdError) as e:
+        sim.set_edge_stiffness(bad)
+    assert e.value.code == pdg.PD_ERR_FACTORIZATION
+    sim.set_edge_stiffness(k)
+    sim.step(6)
+    orc.step(6)
+    if p == 0:
+        assert np.array_equal(bits(sim.state()[0]), bits(orc.state()[0]))
+    else:
+        assert max_rel(sim.state()[0], orc.state()[0]) <= TOL[p]
