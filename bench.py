@@ -26,6 +26,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -136,7 +137,7 @@ def describe_workload(name, scenes, cfgs, precision="mixed"):
 
 # --------------------------------------------------------------------------------- roofline
 def algorithmic_bytes(scene, factor_nnz, iterations, precision="fp64"):
-    """Bytes one substep must move (the per-substep formula stated in the design doc): projection and
+    """Bytes one substep must move: projection and
     scatter, the two triangular solves over the factor's F entries, the residual, prediction and
     velocity update. FP32 projection reads 12-byte positions; an FP32 solve reads 4-byte values."""
     n = scene.n
@@ -199,7 +200,9 @@ def read_peaks():
 class ClockSampler:
     def __init__(self, index):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # the raw samples; PD_BENCH_CLOCKS_DIR keeps them somewhere the caller collects
+        out = os.environ.get("PD_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"clocks_bench_{os.getpid()}.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
