@@ -1,0 +1,215 @@
+"""More of the reference's known answers for the oracle: the scatter's signs and pin-elimination
+term (tests/primitives/test_distance_term.cpp:108-221), the colour-ordered scatter against an
+edge-order sum (:465-506), the bend stencil's matrix rows and constant right-hand side (:961-1012),
+translation invariance (_verify/translation_invariance.cpp) and the pinned chain's analytic
+length change (_verify/chain_test.cpp). Every reference value is restated here from the test's
+description; the expected sums are computed independently in numpy.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def two_vertices(O, pos, pinned, q, k, rest, mass=0.1):
+    mesh = O.Mesh(positions=np.asarray(pos, np.float64), masses=np.full(2, mass),
+                  pinned=np.asarray(pinned, np.uint8), edges=np.array([[0, 1]], np.int32),
+                  edge_rest=np.array([rest]), edge_k=np.array([k]), pin_positions=np.asarray(q, np.float64))
+    return O.OracleSim(mesh, O.Config())
+
+
+def projection(xa, xb, rest):
+    raw = np.asarray(xa, np.float64) - np.asarray(xb, np.float64)
+    ln = math.sqrt(float(raw @ raw))
+    return np.zeros(3) if ln <= 1e-12 else raw * (rest / ln)
+
+
+# ------------------------------------------------ scatter signs (test_distance_term.cpp:108-139)
+def test_scatter_uses_the_standard_pd_sign(oracle):
+    """d = ℓ·unit(x_a − x_b); b_a += κd, b_b −= κd; with a at the origin and b at +0.3ŷ the
+    y components are −κℓ and +κℓ and every other component is zero."""
+    k, rest = 500.0, 0.1
+    pos = [[0.0, 0.0, 0.0], [0.0, 0.3, 0.0]]
+    s = two_vertices(oracle, pos, [0, 0], pos, k, rest)
+    b = s.rhs(np.zeros((2, 3)), overwrite_pins=False).reshape(-1)
+    assert abs(b[1] - (-k * rest)) <= 1e-12 and abs(b[4] - k * rest) <= 1e-12
+    assert b[0] == 0.0 and b[2] == 0.0 and b[3] == 0.0 and b[5] == 0.0
+    assert abs(np.linalg.norm(projection(pos[0], pos[1], rest)) - rest) <= 1e-15
+
+
+# ------------------------------------- pin elimination (test_distance_term.cpp:141-221)
+def test_pin_elimination_adds_kappa_times_the_pin_position(oracle):
+    """One end pinned: the free end's row gains κ·q of the pinned end (its coupling moved to the
+    right-hand side); the pinned row takes nothing; both ends pinned skips the constraint."""
+    k, rest = 300.0, 0.1
+    # (a) vertex 1 pinned at q_1, vertex 0 free somewhere unrelated to q_1
+    pos = [[0.7, -0.2, 0.3], [2.0, 1.0, -4.0]]
+    q = [[0.0, 0.0, 0.0], [2.0, 1.0, -4.0]]
+    s = two_vertices(oracle, pos, [0, 1], q, k, rest)
+    b = s.rhs(np.zeros((2, 3)), overwrite_pins=False)
+    want = k * projection(pos[0], pos[1], rest) + k * np.asarray(q[1])
+    assert np.max(np.abs(b[0] - want)) <= 1e-12 and not np.any(b[1])
+    # (b) vertex 0 pinned, vertex 1 free: the other branch
+    pos = [[-1.5, 0.4, 0.25], [0.0, rest, 0.0]]
+    q = [[-1.5, 0.4, 0.25], [0.0, 0.0, 0.0]]
+    s = two_vertices(oracle, pos, [1, 0], q, k, rest)
+    b = s.rhs(np.zeros((2, 3)), overwrite_pins=False)
+    want = -k * projection(pos[0], pos[1], rest) + k * np.asarray(q[0])
+    assert np.max(np.abs(b[1] - want)) <= 1e-12 and not np.any(b[0])
+    # (c) both pinned: the constraint contributes nothing
+    pos = [[0.0, 0.0, 0.0], [0.0, 2 * rest, 0.0]]
+    s = two_vertices(oracle, pos, [1, 1], pos, k, rest)
+    assert not np.any(s.rhs(np.zeros((2, 3)), overwrite_pins=False))
+
+
+# ------------------------- colour-ordered scatter vs edge order (test_distance_term.cpp:392-506)
+def perturbed_grid(O, n=20, spacing=0.02, k=2.0e3):
+    m = O.make_grid(O.GridSpec(nx=n, ny=n, spacing=spacing, stiffness=k, pin_mode=4))
+    v = np.arange(n * n)
+    i, j = (v % n).astype(np.float64), (v // n).astype(np.float64)
+    m.positions = m.positions + spacing * np.stack([0.20 * np.sin(1.7 * i + 0.5 * j),
+                                                    0.30 * np.cos(0.9 * i - 1.3 * j),
+                                                    0.25 * np.sin(0.4 * i + 2.1 * j)], axis=1)
+    m.pinned = np.zeros(n * n, np.uint8)
+    m.pinned[[0, n * n - 1]] = 1  # both one-end-pinned branches occur
+    m.pin_positions = m.positions.copy()
+    return m
+
+
+def edge_order_scatter(m):
+    """b_a += κd, b_b −= κd, one end pinned adds κ·q to the free end: summed in edge order."""
+    b = np.zeros((m.n, 3))
+    for (a, c), rest, k in zip(m.edges, m.edge_rest, m.edge_k):
+        pa, pc = m.pinned[a], m.pinned[c]
+        if pa and pc:
+            continue
+        d = projection(m.positions[a], m.positions[c], rest)
+        if not pa:
+            b[a] += k * d + (k * m.pin_positions[c] if pc else 0.0)
+        if not pc:
+            b[c] += -k * d + (k * m.pin_positions[a] if pa else 0.0)
+    return b
+
+
+def test_colour_ordered_scatter_matches_the_edge_order_sum(oracle):
+    m = perturbed_grid(oracle)
+    assert m.edges.shape[0] >= 256
+    s = oracle.OracleSim(m, oracle.Config())
+    got = s.rhs(np.zeros((m.n, 3)), overwrite_pins=False)
+    ref = edge_order_scatter(m)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
+    col = s.coloring()
+    assert col["count"] >= 2
+
+
+# ------------------------------- bend stencil rows (test_distance_term.cpp:961-1012)
+def test_bend_stencil_matrix_rows_and_constant_rhs(oracle):
+    """Three points (0,0,0), (0.1, ε, 0), (0.2, 0, 0), outer two pinned, k = 2000: pinned rows are
+    exact identity rows with the pinned columns removed from the free row, the free diagonal is
+    m/h² + 4k (w_b² = 4), and the middle vertex's constant right-hand side is −k·w_b·(q_a + q_c):
+    +800 in x, 0 in y and z; pinned rows take none."""
+    spacing, k, eps, h, mass = 0.1, 2.0e3, 0.01, 1.0 / 120.0, 0.05
+    pos = np.array([[0.0, 0.0, 0.0], [spacing, eps, 0.0], [2 * spacing, 0.0, 0.0]])
+    mesh = oracle.Mesh(positions=pos, masses=np.full(3, mass), pinned=np.array([1, 0, 1], np.uint8),
+                       edges=np.zeros((0, 2), np.int32), edge_rest=np.zeros(0), edge_k=np.zeros(0),
+                       bends=np.array([[0, 1, 2]], np.int32), bend_k=np.array([k]),
+                       pin_positions=np.array([[0.0, 0.0, 0.0], [spacing, eps, 0.0], [2 * spacing, 0.0, 0.0]]))
+    s = oracle.OracleSim(mesh, oracle.Config(dt=h))
+    rp, ci, val = s.matrix()
+    A = np.zeros((3, 3))
+    for r in range(3):
+        A[r, ci[rp[r]:rp[r + 1]]] = val[rp[r]:rp[r + 1]]
+    assert A[0, 0] == 1.0 and A[0, 1] == 0.0 and A[0, 2] == 0.0 and A[1, 0] == 0.0
+    assert A[2, 2] == 1.0 and A[1, 2] == 0.0
+    assert abs(A[1, 1] - (mass / (h * h) + 4.0 * k)) <= 1e-9
+    rhs = s.bend_rhs()
+    assert abs(rhs[1, 0] - 800.0) <= 1e-9 and rhs[1, 1] == 0.0 and rhs[1, 2] == 0.0
+    assert not np.any(rhs[[0, 2]])
+
+
+# ----------------------------------------- translation invariance (_verify/translation_invariance.cpp)
+def spring_at(O, pin, free, gravity):
+    pos = np.array([pin, free], np.float64)
+    mesh = O.Mesh(positions=pos, masses=np.array([0.05, 0.05]), pinned=np.array([1, 0], np.uint8),
+                  edges=np.array([[0, 1]], np.int32), edge_rest=np.array([0.1]), edge_k=np.array([1.0e4]),
+                  velocities=np.zeros((2, 3)), pin_positions=pos.copy())
+    return O.OracleSim(mesh, O.Config(dt=1.0 / 120.0, gravity=gravity, velocity_damping=0.0, max_iterations=40,
+                                      rel_tolerance=0.0, abs_tolerance=1e-18))
+
+
+@pytest.mark.parametrize("pin", [(0, 0, 0), (1, 0, 0), (0, 5, 0), (3, -2, 7)])
+def test_spring_at_rest_length_without_gravity_stays_put(oracle, pin):
+    """At rest length with no gravity the free end does not move (< 1e-12 over 50 substeps),
+    wherever the pin is: a missing κ·q term would pull it toward the origin."""
+    free = np.asarray(pin, np.float64) + [0.0, 0.0, 0.1]
+    s = spring_at(oracle, pin, free, (0.0, 0.0, 0.0))
+    worst = 0.0
+    for _ in range(50):
+        s.step(1)
+        worst = max(worst, float(np.linalg.norm(s.state()[0][1] - free)))
+    assert worst < 1e-12
+
+
+def test_spring_motion_is_translation_invariant(oracle):
+    a = spring_at(oracle, (0, 0, 0), (0, 0.12, 0), (0.0, -9.81, 0.0))
+    b = spring_at(oracle, (10, 20, 30), (10, 20.12, 30), (0.0, -9.81, 0.0))
+    a.step(200)
+    b.step(200)
+    xa, xb = a.state()[0], b.state()[0]
+    assert np.linalg.norm((xa[1] - xa[0]) - (xb[1] - xb[0])) < 1e-9
+
+
+def test_cloth_shape_is_translation_invariant(oracle):
+    """An 8×8 cloth shifted by (5, 7, −3): after 300 substeps every edge length agrees to 1e-6."""
+    runs = []
+    for shift in ((0.0, 0.0, 0.0), (5.0, 7.0, -3.0)):
+        m = oracle.make_grid(oracle.GridSpec(nx=8, ny=8, spacing=0.05, stiffness=1.0e4))
+        m.positions = m.positions + np.asarray(shift)
+        m.pin_positions = m.positions.copy()
+        s = oracle.OracleSim(m, oracle.Config(dt=1.0 / 120.0, max_iterations=20, rel_tolerance=1e-8))
+        s.step(300)
+        x = s.state()[0]
+        runs.append(np.linalg.norm(x[m.edges[:, 0]] - x[m.edges[:, 1]], axis=1))
+    assert np.max(np.abs(runs[0] - runs[1]) / np.maximum(runs[0], 1e-12)) < 1e-6
+
+
+# --------------------------------------------------- hanging chain (_verify/chain_test.cpp)
+def chain(O, n, k, pinned, damping):
+    ell, mass = 0.05, 0.005
+    pos = np.zeros((n, 3))
+    pos[:, 1] = np.arange(n) * ell
+    pin = np.zeros(n, np.uint8)
+    if pinned:
+        pin[0] = 1
+    edges = np.stack([np.arange(n - 1), np.arange(1, n)], axis=1).astype(np.int32)
+    mesh = O.Mesh(positions=pos, masses=np.full(n, mass), pinned=pin, edges=edges, edge_rest=np.full(n - 1, ell),
+                  edge_k=np.full(n - 1, k), velocities=np.zeros((n, 3)), pin_positions=pos.copy())
+    return O.OracleSim(mesh, O.Config(dt=1.0 / 120.0, velocity_damping=damping, max_iterations=40,
+                                      rel_tolerance=0.0, abs_tolerance=1e-16)), edges
+
+
+def chain_length(x, edges):
+    return float(np.sum(np.linalg.norm(x[edges[:, 0]] - x[edges[:, 1]], axis=1)))
+
+
+@pytest.mark.parametrize("n", [5, 20, 100])
+def test_free_chain_falls_without_stretching(oracle, n):
+    s, edges = chain(oracle, n, 1.0e4, False, 0.0)
+    s.step(400)
+    want = (n - 1) * 0.05
+    assert abs(chain_length(s.state()[0], edges) - want) / want < 1e-3
+
+
+@pytest.mark.parametrize("n,k", [(5, 1e4), (5, 1e5), (20, 1e4), (20, 1e5), (100, 1e4), (100, 1e5)])
+def test_pinned_chain_length_matches_the_analytic_sum(oracle, n, k):
+    """The k-th segment from the free end carries k vertices' weight, so the segments change length
+    by m·g·n(n − 1)/(2κ) in total. The chain starts straight above its pin along +y and nothing
+    perturbs it sideways, so it stays a column standing on the pin, compressed by that amount
+    rather than stretched; the reference's 5 % bound on the total length holds either way, and the
+    change itself matches the analytic sum to 1e-6 after 8000 damped substeps."""
+    s, edges = chain(oracle, n, k, True, 0.5)
+    s.step(8000)
+    length = chain_length(s.state()[0], edges)
+    change = 0.005 * 9.81 * n * (n - 1) / (2.0 * k)
+    assert abs(length - ((n - 1) * 0.05 + change)) / ((n - 1) * 0.05 + change) < 0.05
+    assert abs(((n - 1) * 0.05 - length) - change) <= 1e-6 * change
