@@ -213,3 +213,67 @@ def test_pinned_chain_length_matches_the_analytic_sum(oracle, n, k):
     change = 0.005 * 9.81 * n * (n - 1) / (2.0 * k)
     assert abs(length - ((n - 1) * 0.05 + change)) / ((n - 1) * 0.05 + change) < 0.05
     assert abs(((n - 1) * 0.05 - length) - change) <= 1e-6 * change
+
+
+# ------------------------------------------------ projection direction (_verify/direction_audit.cpp)
+def test_projection_direction_follows_the_endpoint_order(oracle):
+    """A: d lies along x_a − x_b (a at the origin, b above ⇒ −ŷ), flips when the order is swapped,
+    and has length ℓ either way (the oracle's projection takes no pin flags, so no pin case can flip it)."""
+    ell = 0.1
+    d1 = oracle.project_one([0.0, 0.0, 0.0], [0.0, 0.15, 0.0], ell)
+    d2 = oracle.project_one([0.0, 0.15, 0.0], [0.0, 0.0, 0.0], ell)
+    assert abs(d1[1] + ell) < 1e-14 and abs(d2[1] - ell) < 1e-14
+    assert abs(np.linalg.norm(d1) - ell) < 1e-15 and abs(np.linalg.norm(d2) - ell) < 1e-15
+
+
+@pytest.mark.parametrize("y", [0.06, 0.08, 0.0999, 0.1001, 0.12, 0.15])
+def test_net_elastic_term_is_the_negative_energy_gradient(oracle, y):
+    """B: with the pin at the origin, the free end's row is (m/h²)·y + κ·y = (m/h²)·ŷ + scatter, so
+    scatter − κ·y must equal −dU/dx = −κ(r − ℓ)·(x_free − x_pin)/r, in stretch and in compression and
+    for both endpoint orders."""
+    k, ell = 1.0e4, 0.1
+    for free_index, pos in ((1, [[0.0, 0.0, 0.0], [0.0, y, 0.0]]), (0, [[0.0, y, 0.0], [0.0, 0.0, 0.0]])):
+        pinned = [1, 0] if free_index == 1 else [0, 1]
+        s = two_vertices(oracle, pos, pinned, pos, k, ell)
+        b = s.rhs(np.zeros((2, 3)), overwrite_pins=False)
+        xf, xp = np.asarray(pos[free_index]), np.asarray(pos[1 - free_index])
+        r = np.linalg.norm(xf - xp)
+        want = (xf - xp) * (-k * (r - ell) / r)
+        assert abs((b[free_index] - k * xf)[1] - want[1]) <= 1e-6
+
+
+def test_scatter_matches_an_independent_standard_pd(oracle):
+    """C: eight arbitrary configurations: b_a = κ·d and b_b = −κ·d with d = ℓ·unit(x_a − x_b)."""
+    k, ell = 1.0e4, 0.1
+    for t in range(8):
+        xa = np.array([0.01 * t, 0.02 + 0.03 * t, -0.015 * t])
+        xb = np.array([-0.005 * t, 0.0, 0.01 * t])
+        s = two_vertices(oracle, [xa, xb], [0, 0], [xa, xb], k, ell)
+        b = s.rhs(np.zeros((2, 3)), overwrite_pins=False)
+        raw = xa - xb
+        d = raw * (ell / np.linalg.norm(raw))
+        assert np.linalg.norm(b[0] - k * d) <= 1e-9 and np.linalg.norm(b[1] + k * d) <= 1e-9
+
+
+# ------------------------------------------------------ bend audit (_verify/bend_audit.cpp:100-186)
+def test_bend_chain_one_implicit_euler_step(oracle):
+    """A three-point chain with only a bend stencil (k = 1000, unit masses, h = 1/120), ends pinned,
+    the middle raised to ŷ = 0.03: pinned rows are exact identity rows (A0), and the solve gives
+    y = ŷ·(m/h²)/(m/h² + 4k) = 0.03·14400/18400 to 1e-12 (A2) with ‖Lx − b‖∞/max(1, ‖b‖∞) < 1e-12 (B)."""
+    k, h, spacing, eps = 1000.0, 1.0 / 120.0, 0.1, 0.03
+    pos = np.array([[0.0, 0.0, 0.0], [spacing, eps, 0.0], [2 * spacing, 0.0, 0.0]])
+    mesh = oracle.Mesh(positions=pos, masses=np.ones(3), pinned=np.array([1, 0, 1], np.uint8),
+                       edges=np.zeros((0, 2), np.int32), edge_rest=np.zeros(0), edge_k=np.zeros(0),
+                       bends=np.array([[0, 1, 2]], np.int32), bend_k=np.array([k]), pin_positions=pos.copy())
+    s = oracle.OracleSim(mesh, oracle.Config(dt=h, gravity=(0.0, 0.0, 0.0)))
+    rp, ci, val = s.matrix()
+    A = np.zeros((3, 3))
+    for r in range(3):
+        A[r, ci[rp[r]:rp[r + 1]]] = val[rp[r]:rp[r + 1]]
+    for v in (0, 2):
+        assert A[v, v] == 1.0 and np.count_nonzero(A[v]) == 1 and A[1, v] == 0.0
+    assert A[1, 1] == 1.0 / (h * h) + 4.0 * k
+    b = s.rhs(pos / (h * h), overwrite_pins=True)
+    x = s.solve(b)
+    assert abs(x[1, 1] - 0.03 * (14400.0 / (14400.0 + 4.0 * k))) < 1e-12
+    assert np.max(np.abs(A @ x - b)) / max(1.0, np.max(np.abs(b))) < 1e-12
