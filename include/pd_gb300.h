@@ -19,10 +19,16 @@
  * message of the calling thread's last failure. Where the reference prints and abort()s on a
  * violated precondition (EigenDirectSolver.cpp:304-314, 363-400), these functions return
  * PD_ERR_INVALID_ARGUMENT / PD_ERR_STATE instead. A factorization failure
- * (EigenDirectSolver.cpp:284-291) returns PD_ERR_FACTORIZATION and leaves the object unready.
+ * (EigenDirectSolver.cpp:284-291) returns PD_ERR_FACTORIZATION: a pd_solver is left unready, as
+ * in the reference; a pd_sim keeps its previous factor and refactorizes at the next stiffness,
+ * mass, pin-mask or dt edit.
  *
  * Threading: a handle is used by one host thread at a time. All device work of a handle is
  * ordered on the handle's CUDA stream.
+ *
+ * Devices: a process uses one GPU, the current device when it first creates a handle. Kernel
+ * attributes (shared-memory limits, non-portable cluster sizes) and co-resident capacities are
+ * set and cached once per process; run one process per GPU for several GPUs.
  */
 #ifndef PD_GB300_H
 #define PD_GB300_H
