@@ -20,8 +20,8 @@
  * violated precondition (EigenDirectSolver.cpp:304-314, 363-400), these functions return
  * PD_ERR_INVALID_ARGUMENT / PD_ERR_STATE instead. A factorization failure
  * (EigenDirectSolver.cpp:284-291) returns PD_ERR_FACTORIZATION: a pd_solver is left unready, as
- * in the reference; a pd_sim keeps its previous factor and refactorizes at the next stiffness,
- * mass, pin-mask or dt edit.
+ * in the reference; a pd_sim keeps its previous factor and refactorizes at its next stiffness
+ * or pin-mask edit (pd_sim_set_edge_stiffness, pd_sim_set_pinned) or dt change (pd_sim_set_config).
  *
  * Threading: a handle is used by one host thread at a time. All device work of a handle is
  * ordered on the handle's CUDA stream.
