@@ -277,3 +277,104 @@ def test_bend_chain_one_implicit_euler_step(oracle):
     x = s.solve(b)
     assert abs(x[1, 1] - 0.03 * (14400.0 / (14400.0 + 4.0 * k))) < 1e-12
     assert np.max(np.abs(A @ x - b)) / max(1.0, np.max(np.abs(b))) < 1e-12
+
+
+# ------------------------------------------ projection definition (test_distance_term.cpp:44-99)
+def test_projection_is_collinear_forward_exact_at_rest_and_zero_when_degenerate(oracle):
+    a, b = np.array([0.1, -0.2, 0.3]), np.array([-0.4, 0.5, -0.6])
+    d = oracle.project_one(a, b, 0.25)
+    raw = a - b
+    assert abs(float(raw @ d) / (np.linalg.norm(raw) * np.linalg.norm(d)) - 1.0) <= 1e-14
+    # at rest length the projection is the edge vector itself, component for component
+    a, b = np.array([1.0, 0.0, 0.0]), np.array([0.63, 0.0, 0.0])
+    assert np.array_equal(oracle.project_one(a, b, 0.37), a - b)
+    # a degenerate edge has no direction: the projection is the zero vector
+    p = np.array([1.0, 2.0, 3.0])
+    assert not np.any(oracle.project_one(p, p, 0.1))
+
+
+def test_projection_energy_gradient_matches_finite_differences(oracle):
+    """E = κ/2·(r − ℓ)² has ∂E/∂x_a = κ(r − ℓ)·(x_a − x_b)/r = κ·((x_a − x_b) − d): the projection
+    d is the point the gradient pulls toward."""
+    k, rest = 1234.0, 0.2
+    pa, pb = np.array([0.1, 0.3, -0.2]), np.array([-0.4, 0.25, 0.35])
+
+    def energy(a):
+        return 0.5 * k * (np.linalg.norm(a - pb) - rest) ** 2
+
+    grad = k * ((pa - pb) - oracle.project_one(pa, pb, rest))
+    for c in range(3):
+        e = np.zeros(3)
+        e[c] = 1e-7
+        fd = (energy(pa + e) - energy(pa - e)) / 2e-7
+        assert abs(grad[c] - fd) <= 1e-6 * abs(fd) + 1e-9
+
+
+# ------------------------------------- refactorization stamp (test_distance_term.cpp:293-330)
+def test_only_left_hand_side_changes_refactorize(oracle):
+    """Pin drags and damping leave Ã alone (no refactorization); stiffness and dt changes refactorize."""
+    pos = np.array([[0.0, 0.0, 0.0], [0.4, 0.1, 0.0]])
+    mesh = oracle.Mesh(positions=pos, masses=np.array([0.1, 0.1]), pinned=np.array([1, 0], np.uint8),
+                       edges=np.array([[0, 1]], np.int32), edge_rest=np.array([0.1]), edge_k=np.array([400.0]),
+                       pin_positions=pos.copy())
+    cfg = oracle.Config(dt=1.0 / 120.0)
+    s = oracle.OracleSim(mesh, cfg)
+    s.step(1)
+    count = s.stats()["factorize_count"]
+    s.set_pin_positions(np.array([[0.7, -0.3, 2.0], [0.4, 0.1, 0.0]]))
+    s.step(1)
+    s.set_config(oracle.Config(dt=1.0 / 120.0, velocity_damping=0.35))
+    s.step(1)
+    assert s.stats()["factorize_count"] == count
+    s.set_edge_stiffness(np.array([401.0]))
+    s.step(1)
+    assert s.stats()["factorize_count"] == count + 1
+    s.set_config(oracle.Config(dt=1.0 / 240.0, velocity_damping=0.35))
+    s.step(1)
+    assert s.stats()["factorize_count"] == count + 2
+
+
+# ------------------------------------------ grid construction (test_distance_term.cpp:769-935)
+def test_shear_diagonals_are_added_once(oracle):
+    nx = ny = 20
+    base = oracle.make_grid(oracle.GridSpec(nx=nx, ny=ny, spacing=0.05))
+    sheared = oracle.make_grid(oracle.GridSpec(nx=nx, ny=ny, spacing=0.05, shear_stiffness=1.0e3))
+    assert base.edges.shape[0] == 2 * nx * ny - nx - ny
+    assert sheared.edges.shape[0] == base.edges.shape[0] + (nx - 1) * (ny - 1)
+    pairs = {tuple(sorted(map(int, e))) for e in sheared.edges}
+    assert len(pairs) == sheared.edges.shape[0]
+    assert np.array_equal(sheared.edges[:base.edges.shape[0]], base.edges)
+
+
+def test_bend_stencils_have_the_exact_vertex_triples(oracle):
+    """Rows first (centre i = 1..nx−2 of every row j, in order), then columns (centre j = 1..ny−2
+    of every column i); every stencil carries the given stiffness; none without a grid bend knob."""
+    nx, ny, k = 20, 14, 777.0
+    assert oracle.make_grid(oracle.GridSpec(nx=nx, ny=ny, spacing=0.05)).bends.shape[0] == 0
+    m = oracle.make_grid(oracle.GridSpec(nx=nx, ny=ny, spacing=0.05, bend_stiffness=k))
+    rows = [(j * nx + i - 1, j * nx + i, j * nx + i + 1) for j in range(ny) for i in range(1, nx - 1)]
+    cols = [((j - 1) * nx + i, j * nx + i, (j + 1) * nx + i) for i in range(nx) for j in range(1, ny - 1)]
+    assert m.bends.shape[0] == (nx - 2) * ny + (ny - 2) * nx
+    assert [tuple(map(int, b)) for b in m.bends] == rows + cols
+    assert np.all(m.bend_k == k)
+
+
+def test_strided_bend_sampling_cannot_see_coarse_bending(oracle):
+    """Stride 2 on a 9×2 grid keeps only the odd row centres (8 stencils); putting every odd vertex
+    at the midpoint of its even neighbours zeroes every sampled A_s·x exactly, however strongly the
+    even sub-grid bends (test_distance_term.cpp:1274-1330): the counterexample for which the
+    reference rejects strided sampling."""
+    nx, ny = 9, 2
+    m = oracle.make_grid(oracle.GridSpec(nx=nx, ny=ny, spacing=1.0, bend_stiffness=1000.0, bend_stride=2,
+                                         pin_mode=4))
+    assert m.bends.shape[0] == 8 and all((int(b[1]) % nx) % 2 == 1 for b in m.bends)
+    even = np.array([0.0, 1.0, 4.0, 9.0, 16.0])
+    y = np.zeros(nx)
+    y[0::2] = even
+    y[1::2] = 0.5 * (even[:-1] + even[1:])
+    x = m.positions.copy()
+    for j in range(ny):
+        x[j * nx:(j + 1) * nx, 1] = y
+    second = x[m.bends[:, 0]] - 2.0 * x[m.bends[:, 1]] + x[m.bends[:, 2]]
+    assert not np.any(second)
+    assert np.all(even[:-2] - 2.0 * even[1:-1] + even[2:] == 2.0)  # the even sub-grid bends throughout
