@@ -1,8 +1,11 @@
 """More of the reference's known answers for the oracle: the scatter's signs and pin-elimination
 term (tests/primitives/test_distance_term.cpp:108-221), the colour-ordered scatter against an
 edge-order sum (:465-506), the bend stencil's matrix rows and constant right-hand side (:961-1012),
-translation invariance (_verify/translation_invariance.cpp) and the pinned chain's analytic
-length change (_verify/chain_test.cpp). Every reference value is restated here from the test's
+translation invariance (_verify/translation_invariance.cpp), the pinned chain's analytic
+length change (_verify/chain_test.cpp), the projection-direction and bend audits
+(_verify/direction_audit.cpp, _verify/bend_audit.cpp), the projection's definition, the refactorization
+stamp and grid construction (test_distance_term.cpp:44-99,293-330,769-935,1274-1330) and the spring
+fixed points (tests/chain/spring_vertical.cpp:130-152,231-252,442-512). Every reference value is restated here from the test's
 description; the expected sums are computed independently in numpy.
 """
 import math
@@ -378,3 +381,55 @@ def test_strided_bend_sampling_cannot_see_coarse_bending(oracle):
     second = x[m.bends[:, 0]] - 2.0 * x[m.bends[:, 1]] + x[m.bends[:, 2]]
     assert not np.any(second)
     assert np.all(even[:-2] - 2.0 * even[1:-1] + even[2:] == 2.0)  # the even sub-grid bends throughout
+
+
+# ------------------------------------------------------ spring fixed points (spring_vertical.cpp)
+def test_iteration_count_does_not_change_the_fixed_point(oracle):
+    """One spring: the projection is −ℓŷ whatever x is and the matrix already holds κ, so one
+    iteration lands on the fixed point: 1, 5 and 50 iterations agree to 1e-15·ℓ and match the
+    closed form to 1e-12 (spring_vertical.cpp:130-152)."""
+    from tests.test_oracle import ELL, H, K, M, closed_form, spring
+    ys = []
+    for iters in (1, 5, 50):
+        s = spring(oracle, 0.12, iters=iters)
+        s.step(1)
+        ys.append(s.state()[0][1, 1])
+    assert abs(ys[2] - closed_form(0.12 - H * H * 9.81, M, K, H)) / ELL <= 1e-12
+    assert abs(ys[1] - ys[2]) / ELL <= 1e-15 and abs(ys[0] - ys[2]) / ELL <= 1e-15
+
+
+@pytest.mark.parametrize("h", [1.0 / 240.0, 1.0 / 480.0, 1.0 / 960.0])
+def test_damped_spring_settles_at_the_energy_minimum(oracle, h):
+    """E(y) = κ/2·(y − ℓ)² + m·g·y is least at y = ℓ − m·g/κ, below the rest length, for every h
+    (spring_vertical.cpp:231-252; κ = 20, damping 0.5, 40 s)."""
+    from tests.test_oracle import ELL, M, spring
+    k = 20.0
+    s = spring(oracle, 0.12, kd=0.5, k=k, h=h)
+    s.step(int(40.0 / h))
+    assert abs(s.state()[0][1, 1] - (ELL - M * 9.81 / k)) / ELL <= 1e-3
+
+
+def test_free_chain_iterates_to_rest_lengths_without_gravity(oracle):
+    """Twelve unpinned vertices on a slanted line, spaced wider than ℓ, one PD iteration a substep,
+    no gravity, damping or early exit: the substep change falls to 1e-12 and every edge returns to
+    its rest length to 1e-9 (spring_vertical.cpp:442-512)."""
+    n, ell, k = 12, 0.1, 1.0e3
+    pos = np.array([[0.03 * i, 0.11 * i, 0.0] for i in range(n)])
+    edges = np.stack([np.arange(n - 1), np.arange(1, n)], axis=1).astype(np.int32)
+    mesh = oracle.Mesh(positions=pos, masses=np.full(n, 0.05), pinned=np.zeros(n, np.uint8), edges=edges,
+                       edge_rest=np.full(n - 1, ell), edge_k=np.full(n - 1, k), velocities=np.zeros((n, 3)),
+                       pin_positions=pos.copy())
+    s = oracle.OracleSim(mesh, oracle.Config(dt=1.0 / 120.0, gravity=(0.0, 0.0, 0.0), velocity_damping=0.0,
+                                             max_iterations=1, rel_tolerance=0.0, abs_tolerance=0.0))
+    x = pos
+    for _ in range(50000):
+        s.step(1)
+        nxt = s.state()[0]
+        change = float(np.max(np.abs(nxt - x)))
+        x = nxt
+        if change <= 1e-12:
+            break
+    assert change <= 1e-12
+    lengths = np.linalg.norm(x[edges[:, 0]] - x[edges[:, 1]], axis=1)
+    assert np.max(np.abs(lengths - ell)) / ell < 1e-9
+    assert abs(lengths.sum() - (n - 1) * ell) <= 1e-9
