@@ -1,7 +1,8 @@
 """The reference's known-answer scenes stepped on the GPU: the pinned chain of
 _verify/chain_test.cpp (a line graph, so an elimination tree unlike a cloth's) and the translated
 springs and cloth of _verify/translation_invariance.cpp (pins away from the origin, where a missing
-κ·q term would show). Each against the oracle on the same scene, plus the scene's own answer.
+κ·q term would show), and the pin-mask change of tests/chain/spring_vertical.cpp that must
+reanalyze. Each against the oracle on the same scene, plus the scene's own answer.
 """
 import numpy as np
 import pytest
@@ -91,3 +92,43 @@ def test_translated_cloth(pdg, p):
         lengths.append(np.linalg.norm(x[e[:, 0]] - x[e[:, 1]], axis=1))
     if p != 4:
         assert np.max(np.abs(lengths[0] - lengths[1]) / np.maximum(lengths[0], 1e-12)) < 1e-6
+
+
+@pytest.mark.parametrize("p", [0, 1, 4])
+def test_pin_mask_change_reanalyzes(pdg, p):
+    """Pinning an interior vertex of a 6×6 cloth mid-run removes its coupling blocks, so Ã's pattern
+    changes: one new analysis and factorization, none after (spring_vertical.cpp:528-560). The
+    stepping after the change matches an oracle started from the state at the change with the new
+    pin mask (the substep depends on x and v alone), bit for bit in reference order."""
+    cfg = pdg.SceneConfig(grid_nx=6, grid_ny=6, grid_spacing=0.05, stiffness=1.0e4, max_iterations=4,
+                          rel_tolerance=0.0, abs_tolerance=0.0, precision=p)
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    sim.step(6)
+    orc.step(6)
+    assert sim.info()["analyze_count"] == 1
+    v = 2 * 6 + 2
+    pinned = np.asarray(scene.pinned, np.uint8).copy()
+    assert pinned[v] == 0
+    pinned[v] = 1
+    sim.set_pinned(pinned)  # the new pin holds its current position
+    info = sim.info()
+    assert info["analyze_count"] == 2 and info["factorize_count"] == 2
+    x, vel = orc.state()
+    q = np.asarray(scene.positions, np.float64).copy()
+    q[v] = x[v]
+    after = pdg.GridScene(positions=x, masses=scene.masses, pinned=pinned, edges=scene.edges,
+                          edge_rest=scene.edge_rest, edge_stiffness=scene.edge_stiffness, velocities=vel,
+                          pin_positions=q)
+    orc2 = oracle_twin(after, cfg, perm=sim.factor()["perm"])
+    sim.step(6)
+    orc2.step(6)
+    info = sim.info()
+    assert info["analyze_count"] == 2 and info["factorize_count"] == 2
+    got = sim.state()[0]
+    assert np.all(np.isfinite(got))
+    if p == 0:
+        assert np.array_equal(bits(got), bits(orc2.state()[0]))
+    else:
+        assert max_rel(got, orc2.state()[0]) <= TOL[p]
