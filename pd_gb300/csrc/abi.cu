@@ -1057,10 +1057,10 @@ struct pd_sim {
 
   // The second stream and its fork/join events, created before any launch (or capture) needs them.
   int ensureAux() {
-    if (corrBig <= 0 || aux) return PD_OK;
-    PD_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
-    PD_CUDA(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
-    PD_CUDA(cudaEventCreateWithFlags(&joinEv, cudaEventDisableTiming));
+    if (corrBig <= 0 || (aux && forkEv && joinEv)) return PD_OK;
+    if (!aux) PD_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));  // each kept once made
+    if (!forkEv) PD_CUDA(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
+    if (!joinEv) PD_CUDA(cudaEventCreateWithFlags(&joinEv, cudaEventDisableTiming));
     return PD_OK;
   }
 
@@ -1928,8 +1928,14 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
   if (const int rc = saveSim(s, o)) return rc;
   const int capacity = std::max(s->logCapacity, substeps);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  PD_CUDA(cudaEventCreate(&e0));
-  PD_CUDA(cudaEventCreate(&e1));
+  {
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+      if (e0) cudaEventDestroy(e0);
+      return cudaFail(ce, "autotune timing events");
+    }
+  }
   std::vector<pd_plan> plans, effective;
   std::vector<double> times;
   int rc = PD_OK;
