@@ -15,8 +15,10 @@ workload's full substep count), ``fp64_gpu`` (the plain one-cloth-per-launch FP6
 same workload) and ``cpu_baseline``. ``--impl reference`` times the CPU oracle (the reference
 algorithm restated) on all host cores instead. Under torchrun each rank steps its own cloth(s)
 (replicas; no collective on the data path) and rank 0 reports the aggregate. The default run
-(N = 1) also carries the metric's other two parts, ``batch512`` (``--workload batch``) and
-``gradients`` (``--workload differentiable``), measured by this script as child processes.
+(N = 1) also carries the metric's other parts, ``batch512`` (``--workload batch``), ``cloth256``
+(the single large cloth) and ``gradients`` (``--workload differentiable``), measured by this script
+as child processes. ``precision_variants`` times the other precision modes on the same workload,
+each with its position error against the oracle.
 """
 from __future__ import annotations
 
@@ -68,7 +70,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=None)  # default: 600 substeps (3 gradient batches)
+    p.add_argument("--steps", type=int, default=None)  # default: 600 substeps, 30 batch substeps, 3 gradient batches
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--workload", default="cloth40_full")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -82,13 +84,19 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-refactor", action="store_true")
     p.add_argument("--no-headline-parts", action="store_true")  # skip the batch / gradient children
+    # other precision modes on the same workload, each timed and checked against the oracle
+    p.add_argument("--variants", default=None, help="comma-separated modes; default per workload, 'none' to skip")
     p.add_argument("--grad-batch", type=int, default=64)       # differentiable workload: problems per launch
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--grad-side", type=int, default=64)         # smaller only for profiling captures
     p.add_argument("--grad-substeps", type=int, default=120)
     a = p.parse_args()
     if a.steps is None:
-        a.steps = 3 if a.workload == "differentiable" else 600
+        a.steps = {"differentiable": 3, "batch": 30}.get(a.workload, 600)
+    if a.variants is None:
+        a.variants = {"cloth40_full": "fp64,fp32-projection,fp32-solve", "cloth40_plain": "fp64,fp32-projection",
+                      "cloth256": "fp64,fp32-projection"}.get(a.workload, "none")
+    a.variants = [] if a.variants == "none" else [m for m in a.variants.split(",") if m and m != a.precision]
     return a
 
 
@@ -125,14 +133,20 @@ def workload(name, batch_count, precision="mixed"):
     return scenes, cfgs, sub
 
 
-def describe_workload(name, scenes, cfgs, precision="mixed"):
+L2_NOTE = ("GPU arm: a 256 MB device write between timed substeps, outside the timed events; "
+           "CPU arms: caches not flushed")
+
+
+def describe_workload(name, scenes, cfgs, substeps):
+    """The workload's description, the same for every arm: built from the cloths' array sizes and
+    the configuration knobs, which the product's scenes and the oracle's meshes both carry."""
     c = cfgs[0]
     n = sum(s.n for s in scenes)
     e = sum(int(s.edges.shape[0]) for s in scenes)
     b = sum(int(np.asarray(s.bends).reshape(-1, 3).shape[0]) for s in scenes)
     return {"workload": name, "instances": len(scenes), "vertices": n, "constraints": e, "bend_stencils": b,
             "iterations": c.max_iterations, "residual_tolerance": c.residual_tolerance, "dt": c.dt,
-            "precision": precision}
+            "substeps_per_run": substeps, "l2": L2_NOTE}
 
 
 # --------------------------------------------------------------------------------- roofline
@@ -197,10 +211,76 @@ def read_peaks():
 
 
 # --------------------------------------------------------------------------------- clocks
+# clocks-event reason bits of NVML (nvml.h: nvmlClocksEventReason*), the ones a run is judged by
+_NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml): SM clock, its maximum and
+    the active clocks-event reasons of one GPU. Never changes a setting."""
+
+    def __init__(self, cuda_index):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.dev = C.c_void_p()
+        bus = None
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(cuda_index)
+            bus = f"{p.pci_domain_id:08x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0".encode()
+        except Exception:  # noqa: BLE001 — older torch: fall back to the index
+            bus = None
+        ok = bus is not None and self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus, C.byref(self.dev)) == 0
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(int(cuda_index), C.byref(self.dev)) != 0:
+            raise OSError("no NVML handle for the device")
+        reasons = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = reasons or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        sm, smax, r = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.dev, 1, C.byref(sm))        # NVML_CLOCK_SM
+        self.lib.nvmlDeviceGetMaxClockInfo(self.dev, 1, C.byref(smax))
+        self.reasons_fn(self.dev, C.byref(r))
+        return float(sm.value), float(smax.value), int(r.value)
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
-    def __init__(self, index):
+    """SM clocks and throttle reasons during a timed region: NVML polled every millisecond from a
+    thread (the timed regions of short runs last a few milliseconds), else nvidia-smi every 100 ms.
+    stop() returns {sm_mhz (median), sm_max_mhz, reasons, samples, source}."""
+
+    def __init__(self, index, period_s=0.001):
+        import threading
+        self.samples = []
         self.proc = None
-        # the raw samples; PD_BENCH_CLOCKS_DIR keeps them somewhere the caller collects
+        self.nvml = None
+        try:
+            self.nvml = _Nvml(index)
+        except Exception:  # noqa: BLE001 — NVML missing: nvidia-smi below
+            self.nvml = None
+        if self.nvml is not None:
+            self.stop_flag = threading.Event()
+
+            def run():
+                while not self.stop_flag.is_set():
+                    try:
+                        self.samples.append(self.nvml.sample())
+                    except Exception:  # noqa: BLE001
+                        break
+                    self.stop_flag.wait(period_s)
+
+            self.samples.append(self.nvml.sample())
+            self.thread = threading.Thread(target=run, daemon=True)
+            self.thread.start()
+            return
         out = os.environ.get("PD_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
         self.path = os.path.join(out, f"clocks_bench_{os.getpid()}.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -216,8 +296,21 @@ class ClockSampler:
             self.proc = None
 
     def stop(self):
+        if self.nvml is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+            try:
+                self.samples.append(self.nvml.sample())
+            except Exception:  # noqa: BLE001
+                pass
+            self.nvml.close()
+            sm = [s[0] for s in self.samples]
+            reasons = sorted({nm for _, _, r in self.samples for bit, nm in _NVML_REASONS.items() if r & bit})
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": max(s[1] for s in self.samples) if sm else None,
+                    "reasons": reasons, "samples": len(sm), "source": "NVML, 1 ms"}
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -239,57 +332,62 @@ class ClockSampler:
                 if val.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 100 ms"}
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_baseline(scenes, cfgs, substeps_total, max_seconds, threads=0):
-    """The oracle on the host cores: substeps/s over a bounded sample of the same workload."""
-    from oracle import oracle as O  # noqa: F401  (checker / baseline only)
-    from tests.helpers import oracle_twin
-    ncores = threads or os.cpu_count()
-    done = 0
-    t_total = 0.0
-    sims = [oracle_twin(s, c, threads=ncores) for s, c in zip(scenes, cfgs)]
-    for s in sims:
-        s.step(1)  # factorization happens in the first step; exclude it
-    for k in range(substeps_total):
+def time_oracle(name, batch_count, warmup, steps, max_seconds=None, threads=0):
+    """The reference algorithm (the oracle's restatement) on the host cores, on the workload built
+    by the oracle alone (``oracle/workloads.py``; the product library is never loaded): `warmup`
+    untimed substeps (at least one: the first substep factorizes), then up to `steps` timed
+    substeps of every cloth, stopping early once `max_seconds` of timed work have run. The same
+    substeps as the GPU arm times: the ones after the warm-up, from the workload's initial state.
+    Returns (meshes, configs, workload substeps, substeps timed, seconds, threads)."""
+    from oracle import oracle as O, workloads as OW  # checker / CPU baseline only
+    ncores = threads or os.cpu_count() or 1
+    meshes, ocfgs, sub = OW.build(name, batch_count, threads=ncores)
+    sims = [O.OracleSim(m, c) for m, c in zip(meshes, ocfgs)]
+    for _ in range(max(1, warmup)):
+        for s in sims:
+            s.step(1)
+    done, t_total = 0, 0.0
+    for _ in range(steps):
         t0 = time.perf_counter()
         for s in sims:
             s.step(1)
         t_total += time.perf_counter() - t0
         done += 1
-        if t_total > max_seconds:
+        if max_seconds is not None and t_total > max_seconds:
             break
-    return {"value": len(sims) * done / t_total, "unit": UNIT, "cores": ncores, "kind": "port",
-            "sample": f"{done} consecutive substeps of the workload ({len(sims)} cloth(s)) on the CPU oracle, "
-                      f"{t_total:.1f} s, OpenMP {ncores} threads"}
+    return meshes, ocfgs, sub, done, t_total, ncores
+
+
+def cpu_baseline(name, batch_count, warmup, steps, max_seconds):
+    """The oracle on the host cores: substeps/s over a bounded sample of the same workload — the
+    substeps the GPU arm times, cut short after `max_seconds`."""
+    meshes, _, _, done, t, ncores = time_oracle(name, batch_count, warmup, steps, max_seconds)
+    return {"value": len(meshes) * done / t, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"substeps {max(1, warmup) + 1}..{max(1, warmup) + done} of the workload "
+                      f"({len(meshes)} cloth(s)) on the CPU oracle, {t:.1f} s, OpenMP {ncores} threads"}
 
 
 def run_reference(args):
+    """The reference arm: the reference algorithm (oracle restatement; the reference itself needs
+    Eigen, which is not installed) on all host cores, timed over exactly `steps` substeps after
+    `warmup`, on the workload built by the oracle alone. Imports nothing of the product."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    scenes, cfgs, sub = workload(args.workload, args.batch_count)
-    from tests.helpers import oracle_twin
-    ncores = os.cpu_count()
-    sims = [oracle_twin(s, c, threads=ncores) for s, c in zip(scenes, cfgs)]
-    for _ in range(args.warmup):
-        for s in sims:
-            s.step(1)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for s in sims:
-            s.step(1)
-    dt = time.perf_counter() - t0
-    value = len(sims) * args.steps / dt  # aggregate (cloth-)substeps/s
+    meshes, ocfgs, sub, done, dt, ncores = time_oracle(args.workload, args.batch_count, args.warmup, args.steps)
+    value = len(meshes) * done / dt  # aggregate (cloth-)substeps/s
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": dt / done * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": describe_workload(args.workload, scenes, cfgs), "impl": "reference",
+            "config": describe_workload(args.workload, meshes, ocfgs, sub), "impl": "reference",
+            "precision": "fp64", "parallelism": f"{ncores} host threads (OpenMP)",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": f"{args.steps} consecutive substeps after {args.warmup} warm-up substeps, "
-                                       f"CPU oracle (reference algorithm restated), OpenMP {ncores} threads"},
+                             "sample": f"substeps {max(1, args.warmup) + 1}..{max(1, args.warmup) + done} of the "
+                                       f"workload, CPU oracle (reference algorithm restated), OpenMP {ncores} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -421,24 +519,90 @@ def stage_shares(P, scenes, cfgs, plan, substeps=20):
     return out
 
 
-def position_error(P, args, scenes, cfgs, substeps, plan=None):
+_ORACLE_FINAL = {}
+
+
+def oracle_final(P, name, scenes, cfgs, substeps, picks):
+    """Final positions of the FP64 CPU oracle after `substeps` substeps from the initial state, for
+    the cloths `picks` (each with the elimination order the GPU handle uses); computed once per
+    workload and kept, so that every precision mode is compared with the same reference run."""
+    from tests.helpers import oracle_twin  # checker only
+    out = {}
+    for i in picks:
+        key = (name, i, substeps)
+        if key not in _ORACLE_FINAL:
+            c = copy.copy(cfgs[i])
+            c.precision = PRECISIONS["fp64"][0]
+            probe = P.Simulator([scenes[i]], [c])
+            perm = probe.factor(0)["perm"]
+            probe.close()
+            orc = oracle_twin(scenes[i], cfgs[i], perm=perm, threads=os.cpu_count())
+            orc.step(substeps)
+            _ORACLE_FINAL[key] = orc.state()[0]
+        out[i] = _ORACLE_FINAL[key]
+    return out
+
+
+def position_error(P, args, scenes, cfgs, substeps, plan=None, bound=POS_ERR_BOUND):
     """max |x_gpu − x_oracle| / max |x_oracle| after `substeps` substeps from the initial state, this
     precision mode against the FP64 CPU oracle, for the run as timed: every cloth on one handle with
     the timed launch plan; checked on cloth 0 and on the largest cloth."""
-    from tests.helpers import max_rel, oracle_twin  # checker only
+    from tests.helpers import max_rel  # checker only
     sim = P.Simulator(scenes, cfgs)
     if plan is not None:
         sim.set_plan(plan)
     sim.step(substeps)
     picks = sorted({0, int(np.argmax([sc.n for sc in scenes]))})
-    errs = {}
-    for i in picks:
-        orc = oracle_twin(scenes[i], cfgs[i], perm=sim.factor(i)["perm"], threads=os.cpu_count())
-        orc.step(substeps)
-        errs[str(i)] = max_rel(sim.state(i)[0], orc.state()[0])
+    want = oracle_final(P, args.workload, scenes, cfgs, substeps, picks)
+    errs = {str(i): max_rel(sim.state(i)[0], want[i]) for i in picks}
     err = max(errs.values())
-    return {"value": err, "bound": POS_ERR_BOUND, "within": bool(err <= POS_ERR_BOUND), "substeps": substeps,
+    return {"value": err, "bound": bound, "within": bool(err <= bound), "substeps": substeps,
             "cloths": errs, "against": "FP64 CPU oracle (reference algorithm restated), cloths of the run as timed"}
+
+
+def time_mode(P, args, stream, flush, precision, max_steps=50):
+    """Substeps/s of one precision mode on the workload, timed like `value` (autotuned plan, one
+    launch per substep, L2 flushed between substeps, CUDA events on the simulator's stream)."""
+    import torch
+    scenes, cfgs, _ = workload(args.workload, args.batch_count, precision)
+    sim = P.Simulator(scenes, cfgs)
+    sim.set_stream(stream.cuda_stream)
+    if not args.no_autotune:
+        sim.autotune(3)
+    k = min(args.steps, max_steps)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sim.step(1, sync=False)
+            flush.fill_(1.0)
+        for j in range(k):
+            flush.fill_(float(j))
+            starts[j].record(stream)
+            sim.step(1, sync=False)
+            ends[j].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / k
+    info = sim.info(0)
+    return {"value": len(scenes) * 1e3 / ms, "unit": UNIT, "ms_per_step": ms, "steps": k,
+            "kernel": kernel_name(info), "ctas_per_cloth": info["cluster_ctas"], "plan": sim.plan(),
+            "dtype": PRECISIONS[precision][1]}, scenes, cfgs
+
+
+def precision_variants(P, args, stream, flush, modes, substeps):
+    """The workload in each of `modes`: throughput timed like `value` and the position error against
+    the FP64 CPU oracle after the workload's `substeps` (with the timed plan). FP64's bar is 1e-10,
+    the reduced-precision modes' 1e-5."""
+    out = {}
+    for mode in modes:
+        try:
+            line, scenes, cfgs = time_mode(P, args, stream, flush, mode)
+            bound = 1e-10 if PRECISIONS[mode][0] <= 1 else POS_ERR_BOUND
+            line["pos_err"] = position_error(P, args, scenes, cfgs, substeps, line["plan"], bound)
+        except Exception as e:  # noqa: BLE001 — reported in the line, the main result stands
+            line = {"error": f"{type(e).__name__}: {e}"[:300]}
+        out[mode] = line
+    return out
 
 
 def headline_parts(args):
@@ -447,6 +611,7 @@ def headline_parts(args):
     the default run's JSON line. A part that fails is reported with its error."""
     parts = {}
     runs = {"batch512": ["--workload", "batch", "--steps", "30", "--no-cpu-baseline"],
+            "cloth256": ["--workload", "cloth256", "--steps", "20", "--no-cheb", "--cpu-sample-seconds", "5"],
             "gradients": ["--workload", "differentiable", "--steps", "1", "--no-cpu-baseline"]}
     for name, extra in runs.items():
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--warmup", str(args.warmup)] + extra
@@ -457,7 +622,8 @@ def headline_parts(args):
             parts[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
             continue
         keep = ("value", "unit", "ms_per_step", "e2e", "roofline", "pos_err", "fp64_gpu", "fp64_gpu_batched",
-                "grad_check", "fp64", "cpu_baseline", "clocks", "config", "plan", "autotune")
+                "grad_check", "fp64", "cpu_baseline", "clocks", "config", "precision", "kernel", "plan", "autotune",
+                "refactor", "precision_variants")
         parts[name] = {k: line[k] for k in keep if k in line}
         parts[name]["command"] = " ".join(["python", "bench.py", "--warmup", str(args.warmup)] + extra)
     return parts
@@ -569,11 +735,11 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": PRECISIONS[args.precision][1], "data": "synthetic",
-                "config": dict(describe_workload(args.workload, scenes, cfgs, args.precision),
-                               l2="flushed between timed substeps (256 MB device write outside the timed events)",
-                               parallelism=f"replicas x{world}" if world > 1 else "single GPU",
-                               kernel=kernel, ctas_per_cloth=info["cluster_ctas"],
-                               factor_nnz=info["factor_nnz"], iterations_used=iters_used[0]),
+                "config": describe_workload(args.workload, scenes, cfgs, sub),
+                "precision": args.precision,
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                "kernel": {"name": kernel, "ctas_per_cloth": info["cluster_ctas"], "factor_nnz": info["factor_nnz"],
+                           "iterations_used_last_timed_substep": iters_used[0]},
                 "wall_s": t_wall,
                 "gpu_launches": args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -600,8 +766,11 @@ def run_ours(args):
             line["pos_err"] = pos_err
         if len(scenes) == 1 and not args.no_cheb:
             line["chebyshev"] = chebyshev_line(P, args, stream, flush)
+        if args.variants:
+            line["precision_variants"] = precision_variants(P, args, stream, flush, args.variants, sub)
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(scenes, cfgs, sub, args.cpu_sample_seconds)
+            line["cpu_baseline"] = cpu_baseline(args.workload, args.batch_count, args.warmup, args.steps,
+                                                args.cpu_sample_seconds)
         if args.workload == "cloth40_full" and world == 1 and not args.no_headline_parts:
             del sim  # free the device before the children run
             line.update(headline_parts(args))
@@ -699,9 +868,17 @@ def run_gradients(args):
     g0 = grads[0]
     dirs = [(k0 * rng.normal(0.0, FD_SCALE, k0.shape), rng.normal(0.0, FD_SCALE, (scene.n, 3)),
              weight * rng.normal(0.0, FD_SCALE, (scene.n, 3))) for _ in range(args.fd_directions)]
-    fd_err = {}
-    for eps in (1e-6, 1e-5):
-        fd_sim = P.Simulator([scene] * (2 * len(dirs)), [cfg] * (2 * len(dirs)))
+    # directional derivatives of the adjoint, and the scale ‖g‖·‖d‖ of each (per parameter group)
+    adjs = np.array([g0["dkappa"] @ dk + np.sum(g0["dv0"] * dv) + np.sum(g0["dforce"] * df) for dk, dv, df in dirs])
+    scales = np.array([np.linalg.norm(g0["dkappa"]) * np.linalg.norm(dk) + np.linalg.norm(g0["dv0"]) * np.linalg.norm(dv)
+                       + np.linalg.norm(g0["dforce"]) * np.linalg.norm(df) for dk, dv, df in dirs])
+    # central differences D(ε) at a ladder of steps, each ladder rung one batched launch of 2 problems
+    # a direction (loss only); Richardson's R(ε) = (4·D(ε/2) − D(ε))/3 cancels the O(ε²) term, so a
+    # larger ε (less amplified rounding noise) keeps the truncation error small
+    ladder = (1e-6, 5e-6, 1e-5, 2e-5, 5e-5, 1e-4, 2e-4)
+    D = {}
+    fd_sim = P.Simulator([scene] * (2 * len(dirs)), [cfg] * (2 * len(dirs)))
+    for eps in ladder:
         forces = []
         for j, (dk, dv, df) in enumerate(dirs):
             for s, sign in enumerate((1.0, -1.0)):
@@ -710,22 +887,19 @@ def run_gradients(args):
                 fd_sim.set_state(i, scene.positions, sign * eps * dv)
                 forces.append(sign * eps * df)
         losses = fd_sim.gradient(S, [targets[0]] * (2 * len(dirs)), forces, grad=False)
-        errs, errs_n, fds, adjs = [], [], [], []
-        for j, (dk, dv, df) in enumerate(dirs):
-            fd = (losses[2 * j]["loss"] - losses[2 * j + 1]["loss"]) / (2 * eps)
-            adj = g0["dkappa"] @ dk + np.sum(g0["dv0"] * dv) + np.sum(g0["dforce"] * df)
-            # relative to the directional derivative, and to its scale ‖g‖·‖d‖ per parameter group
-            scale = (np.linalg.norm(g0["dkappa"]) * np.linalg.norm(dk) + np.linalg.norm(g0["dv0"]) * np.linalg.norm(dv)
-                     + np.linalg.norm(g0["dforce"]) * np.linalg.norm(df))
-            errs.append(abs(fd - adj) / max(abs(adj), 1e-300))
-            errs_n.append(abs(fd - adj) / max(scale, 1e-300))
-            fds.append(fd)
-            adjs.append(adj)
-        fds, adjs = np.array(fds), np.array(adjs)
-        fd_err[f"eps_{eps:g}"] = {"max_rel": float(max(errs)), "median_rel": float(np.median(errs)),
-                                  "normwise_rel": float(np.linalg.norm(fds - adjs) / max(np.linalg.norm(adjs), 1e-300)),
-                                  "max_rel_to_gradient_scale": float(max(errs_n))}
-        del fd_sim
+        D[eps] = np.array([(losses[2 * j]["loss"] - losses[2 * j + 1]["loss"]) / (2 * eps) for j in range(len(dirs))])
+    del fd_sim
+
+    def fd_stats(fds):
+        errs = np.abs(fds - adjs) / np.maximum(np.abs(adjs), 1e-300)
+        return {"max_rel": float(errs.max()), "median_rel": float(np.median(errs)),
+                "directions_within_1e-6": int(np.sum(errs <= 1e-6)),
+                "normwise_rel": float(np.linalg.norm(fds - adjs) / max(np.linalg.norm(adjs), 1e-300)),
+                "max_rel_to_gradient_scale": float(np.max(np.abs(fds - adjs) / np.maximum(scales, 1e-300)))}
+
+    fd_err = {f"eps_{eps:g}": fd_stats(D[eps]) for eps in ladder}
+    fd_err["richardson"] = {f"eps_{eps:g}": fd_stats((4.0 * D[eps / 2] - D[eps]) / 3.0)
+                            for eps in ladder if eps / 2 in D}
     # FP64 CPU reference gradient of problem 0
     orc = oracle_twin(scene, cfg, perm=sim.factor(0)["perm"])
     tc = time.perf_counter()

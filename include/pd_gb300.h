@@ -23,7 +23,8 @@
  * in the reference; a pd_sim keeps its previous factor and refactorizes at its next stiffness
  * or pin-mask edit (pd_sim_set_edge_stiffness, pd_sim_set_pinned) or dt change (pd_sim_set_config).
  *
- * Threading: a handle is used by one host thread at a time. All device work of a handle is
+ * Threading: a handle is used by one host thread at a time, except pd_solver_solve_component,
+ * which three threads may call at once for the three components. All device work of a pd_sim is
  * ordered on the handle's CUDA stream.
  *
  * Devices: a process uses one GPU, the current device when it first creates a handle. Kernel
@@ -52,8 +53,11 @@ extern "C" {
 #define PD_PRECISION_FP64 1       /* FP64, supernodal solve (reordered sums, FMA); matches to rounding */
 #define PD_PRECISION_FP32_PROJECTION 2 /* projection in FP32 accumulated into an FP64 b; FP64 solve */
 #define PD_PRECISION_FP32_SOLVE 3 /* FP32 supernodal solve + one FP64 iterative-refinement step */
-#define PD_PRECISION_MIXED 4      /* FP32 projection and FP32 solve + one FP64 refinement step; small
-                                     cloths: FP32 correction b − Ã·x and FP32 inverse, FP64 positions */
+#define PD_PRECISION_MIXED 4      /* FP32 arithmetic in correction form: each PD iteration adds
+                                     Ã⁻¹·(b − Ã·x), computed in FP32, to positions kept as FP32 hi/lo
+                                     pairs (~48-bit significands); the explicit FP32 inverse for small
+                                     cloths, an FP32 supernodal solve above; state read and written
+                                     as FP64 */
 
 /* Mirror of SceneConfig (core/sim/Scene.h:14-137) plus the fields the synthetic scenes need. */
 typedef struct pd_scene_config {
@@ -175,9 +179,13 @@ int pd_solver_factorize(pd_solver* s, int32_t n, const int32_t* col_ptr, const i
 int pd_solver_analyzed(const pd_solver* s);
 /* IGlobalSolver::solve(b, x) (:66): host vectors of length n; blocks until x is written. */
 int pd_solver_solve(pd_solver* s, const double* b, double* x);
-/* IGlobalSolver::parallelComponents() (:85): 3 for L = Ã ⊗ I₃. */
+/* IGlobalSolver::parallelComponents() (:85): 3 once analysed (L = Ã ⊗ I₃), else 1. */
 int pd_solver_parallel_components(const pd_solver* s);
-/* IGlobalSolver::solveComponent(c, b, x) (:94-97): writes only entries 3v+c of x. */
+/* IGlobalSolver::solveComponent(c, b, x) (:94-97): solves column c alone — reads entries 3v+c of
+ * b, writes only entries 3v+c of x — on the component's own device buffers and stream, so the
+ * three components may be solved from three host threads at once, as the reference's Integrator
+ * does (core/sim/Integrator.cpp:558-565). Calls for one component must not overlap. Each column
+ * is bit-identical to that column of pd_solver_solve. */
 int pd_solver_solve_component(pd_solver* s, int32_t c, const double* b, double* x);
 /* IGlobalSolver::noteSolveStage(seconds) (:111). */
 int pd_solver_note_solve_stage(pd_solver* s, double seconds);
@@ -336,7 +344,12 @@ int pd_sim_set_pin_positions(pd_sim* s, int32_t instance, const double* pin_posi
 int pd_sim_set_edge_stiffness(pd_sim* s, int32_t instance, const double* edge_stiffness);
 /* Changes the pin mask; re-analyzes and refactorizes (Assembler.cpp:149-174). */
 int pd_sim_set_pinned(pd_sim* s, int32_t instance, const uint8_t* pinned, const double* pin_positions);
-/* Replaces the stepping knobs of every instance (dt change ⇒ refactorization). */
+/* Replaces the stepping knobs of every instance (SceneConfig edits between frames). The state is
+ * kept. A dt change refactorizes (dt is part of L). A precision change refactorizes on the host,
+ * drops the launch plan (pd_sim_set_plan / pd_sim_autotune) and re-plans, so the handle then
+ * steps exactly as one created in the new mode from the same state. A cluster_ctas or
+ * dense_max_vertices change re-plans and lays the device arena out again. Other fields (iteration
+ * budget, tolerances, damping, Chebyshev knobs) take effect at the next step. */
 int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg);
 int pd_sim_get_info(pd_sim* s, int32_t instance, pd_sim_info* out);
 int pd_sim_get_stats(pd_sim* s, int32_t instance, pd_sim_stats* out);
@@ -395,7 +408,13 @@ int pd_scene_coloring(const pd_mesh* mesh, uint32_t* color_of, int32_t* colors);
  * - Every call shares the one workspace: calls whose work overlaps on the GPU (different
  *   streams, or different host threads on one device) race; serialise them on one stream.
  *   The workspace needs no clearing: each call overwrites all of it that it reads.
- * - The arithmetic follows the reference's solve order, so x is bit-identical to pd_sim_solve.
+ * - The arithmetic follows the reference's solve order, so x is bit-identical to pd_sim_solve on
+ *   an FP64_EXACT handle; other precision modes' pd_sim_solve uses the supernodal FP64 solve and
+ *   agrees with it to about 1e-10 relative.
+ * - rowidx and val may be NULL only for n = 1 (a factor without off-diagonal entries otherwise
+ *   still needs two non-null device pointers).
+ * - The workspace address is cached per device for the process; after cudaDeviceReset (or any
+ *   other reset of the device's primary context) reload the library before calling again.
  * The work is queued on `stream` (a cudaStream_t; NULL = default stream) and the call returns
  * without waiting. */
 #define PD_NOALLOC_MAX_VERTICES 65536

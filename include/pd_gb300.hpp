@@ -12,7 +12,6 @@
 #pragma once
 
 #include <cstdint>
-#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -226,6 +225,23 @@ class SimContext {
     timing_ = on;
   }
 
+  // Field by field (a byte compare would also see the struct's padding, which c() leaves
+  // unspecified, and call pd_sim_set_config on every substep).
+  static bool sameConfig(const pd_scene_config& a, const pd_scene_config& b) {
+    return a.dt == b.dt && a.substeps_per_frame == b.substeps_per_frame && a.gravity[0] == b.gravity[0] &&
+           a.gravity[1] == b.gravity[1] && a.gravity[2] == b.gravity[2] && a.stiffness == b.stiffness &&
+           a.density == b.density && a.velocity_damping == b.velocity_damping &&
+           a.max_iterations == b.max_iterations && a.rel_tolerance == b.rel_tolerance &&
+           a.abs_tolerance == b.abs_tolerance && a.residual_tolerance == b.residual_tolerance &&
+           a.grid_nx == b.grid_nx && a.grid_ny == b.grid_ny && a.grid_spacing == b.grid_spacing &&
+           a.shear_stiffness == b.shear_stiffness && a.bend_stiffness == b.bend_stiffness &&
+           a.bend_sampling == b.bend_sampling && a.bend_stride == b.bend_stride && a.mass_mode == b.mass_mode &&
+           a.total_mass == b.total_mass && a.pin_mode == b.pin_mode && a.precision == b.precision &&
+           a.cluster_ctas == b.cluster_ctas && a.dense_max_vertices == b.dense_max_vertices &&
+           a.cheb_mode == b.cheb_mode && a.cheb_rho == b.cheb_rho && a.cheb_start == b.cheb_start &&
+           a.cheb_m == b.cheb_m && a.cheb_d == b.cheb_d;
+  }
+
   // What the reference's stepOnce reads from the context at each substep: edits of the pin
   // targets go to the GPU as RHS changes; edits of the stiffnesses, the pin mask or dt refactorize
   // there (the reference's stamp rule, core/assemble/Assembler.cpp:111-174). Bending stiffness
@@ -252,7 +268,7 @@ class SimContext {
       lastPins_ = mesh.pinPositions;
     }
     const pd_scene_config c = config.c();
-    if (std::memcmp(&c, &lastCfg_, sizeof(c)) != 0) {
+    if (!sameConfig(c, lastCfg_)) {
       check(pd_sim_set_config(h_, &c));
       lastCfg_ = c;
     }

@@ -1160,10 +1160,27 @@ struct pd_solver {
   double* dX = nullptr;
   cudaStream_t stream = nullptr;
   pd_solver_stats stats{};
+  // per-component slots of solveComponent (IGlobalSolver.h:94-97: the three components may be
+  // solved from three threads at once): component c owns dCol[3m·c, 3m·(c+1)) on the device
+  // (b, x, workspace), hCol[2m·c, 2m·(c+1)) in page-locked host memory (b, x) and colStream[c]
+  double* dCol = nullptr;
+  double* hCol = nullptr;
+  size_t colM = 0;
+  cudaStream_t colStream[3] = {nullptr, nullptr, nullptr};
+  void releaseColumns() {
+    if (dCol) cudaFree(dCol);
+    if (hCol) cudaFreeHost(hCol);
+    dCol = nullptr;
+    hCol = nullptr;
+    colM = 0;
+  }
   ~pd_solver() {
     if (dArena) cudaFree(dArena);
     if (dDesc) cudaFree(dDesc);
     if (dB) cudaFree(dB);  // dX points into the same allocation
+    releaseColumns();
+    for (cudaStream_t& st : colStream)
+      if (st) cudaStreamDestroy(st);
   }
 };
 
@@ -1673,16 +1690,26 @@ int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
     return fail(PD_ERR_UNSUPPORTED, "unsupported precision mode");
   if (cfg->cheb_mode < PD_CHEB_OFF || cfg->cheb_mode > PD_CHEB_INTERVAL)
     return fail(PD_ERR_INVALID_ARGUMENT, "cheb_mode must be 0, 1 or 2");
-  bool refactor = false;
+  bool refactor = false;  // dt is part of L: a new factor
+  bool arith = false;     // a new precision mode: a host factorization (FP64_EXACT's bits) and a new plan
+  bool replan = false;    // a new CTA count or explicit-inverse limit: a new plan and arena layout
   for (auto& I : s->inst) {
     refactor = refactor || (std::memcmp(&I.cfg.dt, &cfg->dt, sizeof(double)) != 0);
-    I.cfg = *cfg;
+    arith = arith || I.cfg.precision != cfg->precision;
+    replan = replan || I.cfg.cluster_ctas != cfg->cluster_ctas || I.cfg.dense_max_vertices != cfg->dense_max_vertices;
   }
-  if (refactor) {
+  if (refactor || arith || replan) {
+    // the planner and the arena layout depend on these fields, so the state comes back to the
+    // host before the configuration changes and the handle is laid out again from it
     int rc = s->pullState();
     if (rc) return rc;
+    for (auto& I : s->inst) I.cfg = *cfg;
+    if (arith) s->plan = pd_plan{};  // a launch plan is tuned for one mode: the planner's choices apply
     for (auto& I : s->inst) {
+      if (!refactor && !arith) break;
       const auto t0 = Clock::now();
+      // a precision change refactorizes on the host, as a handle created in the new mode does
+      if (arith) I.F.maxRowLen = 0;
       const std::string err = prepare(I, false);
       if (!err.empty()) return fail(PD_ERR_FACTORIZATION, err);
       I.assembleSeconds += secondsSince(t0);
@@ -1694,6 +1721,7 @@ int pd_sim_set_config(pd_sim* s, const pd_scene_config* cfg) {
     return rc;
   }
   if (const int rc_ = s->sync()) return rc_;
+  for (auto& I : s->inst) I.cfg = *cfg;
   return s->writeDescriptors();
 }
 
@@ -2350,6 +2378,14 @@ int pd_solver_factorize(pd_solver* s, int32_t n, const int32_t* cp, const int32_
   d.w = reinterpret_cast<double*>(P(oW));
   if (!s->dDesc) PD_CUDA(cudaMalloc(&s->dDesc, sizeof(pdg::InstanceDev)));
   PD_CUDA(cudaMemcpy(s->dDesc, &d, sizeof(d), cudaMemcpyHostToDevice));
+  if (s->colM != m) {  // the per-component slots, made here so that concurrent solves allocate nothing
+    s->releaseColumns();
+    PD_CUDA(cudaMalloc(&s->dCol, sizeof(double) * 9 * m));
+    PD_CUDA(cudaMallocHost(&s->hCol, sizeof(double) * 6 * m));
+    s->colM = m;
+  }
+  for (cudaStream_t& st : s->colStream)
+    if (!st) PD_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   s->ready = true;
   s->stats.last_factorize_seconds = secondsSince(t0);
   s->stats.total_factorize_seconds += s->stats.last_factorize_seconds;
@@ -2358,7 +2394,7 @@ int pd_solver_factorize(pd_solver* s, int32_t n, const int32_t* cp, const int32_
   return PD_OK;
 }
 
-static int solverSolve(pd_solver* s, const double* b, double* x, int component) {
+static int solverSolve(pd_solver* s, const double* b, double* x) {
   if (!s || !b || !x) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
   if (!s->ready) return fail(PD_ERR_STATE, "solve before a successful factorize");
   const size_t m = s->A.n, bytes = 24 * m;
@@ -2366,21 +2402,14 @@ static int solverSolve(pd_solver* s, const double* b, double* x, int component) 
   const int smem = (24 * static_cast<int>(m) <= kMaxSmem) ? 24 * static_cast<int>(m) : 0;
   const int rc = pdg::launchSolveExact(s->dDesc, s->dB, s->dX, smem, s->stream);
   if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "solve launch");
-  if (component < 0) {
-    PD_CUDA(cudaMemcpyAsync(x, s->dX, bytes, cudaMemcpyDeviceToHost, s->stream));
-    PD_CUDA(cudaStreamSynchronize(s->stream));
-  } else {
-    std::vector<double> tmp(3 * m);
-    PD_CUDA(cudaMemcpyAsync(tmp.data(), s->dX, bytes, cudaMemcpyDeviceToHost, s->stream));
-    PD_CUDA(cudaStreamSynchronize(s->stream));
-    for (size_t v = 0; v < m; ++v) x[3 * v + component] = tmp[3 * v + component];
-  }
+  PD_CUDA(cudaMemcpyAsync(x, s->dX, bytes, cudaMemcpyDeviceToHost, s->stream));
+  PD_CUDA(cudaStreamSynchronize(s->stream));
   return PD_OK;
 }
 
 int pd_solver_solve(pd_solver* s, const double* b, double* x) {
   const auto t0 = Clock::now();
-  const int rc = solverSolve(s, b, x, -1);
+  const int rc = solverSolve(s, b, x);
   if (rc == PD_OK) {
     s->stats.solve_calls += 1;
     s->stats.last_solve_seconds = secondsSince(t0);
@@ -2393,11 +2422,31 @@ int pd_solver_parallel_components(const pd_solver* s) { return (s && s->analyzed
 
 int pd_solver_solve_component(pd_solver* s, int32_t c, const double* b, double* x) {
   if (c < 0 || c > 2) return fail(PD_ERR_INVALID_ARGUMENT, "component out of range");
-  return solverSolve(s, b, x, c);
+  if (!s || !b || !x) return fail(PD_ERR_INVALID_ARGUMENT, "null argument");
+  if (!s->ready) return fail(PD_ERR_STATE, "solve before a successful factorize");
+  // only column c: its entries of b in, its entries of x out, on the component's own stream and
+  // buffers, so the three components run side by side and write disjoint entries of x
+  const size_t m = s->A.n;
+  double* hb = s->hCol + 2 * m * c;
+  double* hx = hb + m;
+  double* db = s->dCol + 3 * m * c;
+  double* dx = db + m;
+  double* dw = dx + m;
+  const cudaStream_t st = s->colStream[c];
+  for (size_t v = 0; v < m; ++v) hb[v] = b[3 * v + c];
+  PD_CUDA(cudaMemcpyAsync(db, hb, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  const int smem = (8 * static_cast<int>(m) <= kMaxSmem) ? 8 * static_cast<int>(m) : 0;
+  const int rc = pdg::launchSolveColumnExact(s->dDesc, db, dx, dw, smem, st);
+  if (rc != 0) return cudaFail(static_cast<cudaError_t>(rc), "component solve launch");
+  PD_CUDA(cudaMemcpyAsync(hx, dx, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+  PD_CUDA(cudaStreamSynchronize(st));
+  for (size_t v = 0; v < m; ++v) x[3 * v + c] = hx[v];
+  return PD_OK;
 }
 
 int pd_solver_note_solve_stage(pd_solver* s, double seconds) {
   if (!s) return fail(PD_ERR_INVALID_ARGUMENT, "null handle");
+  if (pd_solver_parallel_components(s) <= 1) return PD_OK;  // solve() already counted (IGlobalSolver.h:100-111)
   s->stats.solve_calls += 1;
   s->stats.last_solve_seconds = seconds;
   s->stats.total_solve_seconds += seconds;

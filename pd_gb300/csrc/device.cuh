@@ -187,6 +187,10 @@ int launchSubstepExact(const InstanceDev* dInstances, int count, int substeps, i
 // Reference-order FP64 3-column solve for one instance: b (3n, vertex order) → x.
 int launchSolveExact(const InstanceDev* dInstance, const double* b, double* x, int smemBytes,
                      void* stream);
+// One column of that solve: b, x of n doubles in vertex order; w an n-double workspace used when
+// 8n bytes exceed smemBytes. Bit-identical to the matching column of launchSolveExact.
+int launchSolveColumnExact(const InstanceDev* dInstance, const double* b, double* x, double* w, int smemBytes,
+                           void* stream);
 // FP64 substep with the supernodal solve (smem: 6n doubles when they fit).
 int launchSubstepFast(const InstanceDev* dInstances, int count, int substeps, int smemBytes, void* stream,
                       bool timed = false);

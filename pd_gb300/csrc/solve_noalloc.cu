@@ -9,9 +9,11 @@
 //
 // Arithmetic follows the reference's solve exactly (EigenDirectSolver.cpp:411-448): forward
 // sweep column by column in scatter form, then D⁻¹, then the backward sweep gathering each
-// column in ascending row order — so the result is bit-identical to pd_sim_solve.
+// column in ascending row order — so the result is bit-identical to pd_sim_solve on a handle in
+// the FP64_EXACT mode (whose solve follows the same order).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/pd_gb300.h"
@@ -25,8 +27,12 @@ namespace {
 // The shared workspace: 3 doubles per vertex, at most PD_NOALLOC_MAX_VERTICES vertices (1.5 MiB).
 static __device__ __align__(256) double g_noallocScratch[3 * PD_NOALLOC_MAX_VERTICES];
 
+// The workspace's device address per device ordinal, looked up by the first call on that device.
+// Atomic: two host threads making their first call together both store the same address. The
+// address belongs to the device's primary context; after that context is reset (cudaDeviceReset)
+// the library must be reloaded before the next call, which this cache does not detect.
 constexpr int kMaxDevices = 64;
-double* g_scratchAddr[kMaxDevices] = {nullptr};
+std::atomic<double*> g_scratchAddr[kMaxDevices] = {};
 
 // One warp per x/y/z component; the three components never touch each other's entries.
 __global__ void __launch_bounds__(96) solveNoAllocKernel(int n, const int32_t* __restrict__ perm,
@@ -66,7 +72,7 @@ __global__ void __launch_bounds__(96) solveNoAllocKernel(int n, const int32_t* _
 extern "C" int pd_solve_noalloc(int32_t n, const int32_t* perm, const int32_t* colptr, const int32_t* rowidx,
                                 const double* val, const double* dinv, const double* b, double* x,
                                 void* stream) {
-  if (n <= 0 || !perm || !colptr || !dinv || !b || !x) {
+  if (n <= 0 || !perm || !colptr || !dinv || !b || !x || (n > 1 && (!rowidx || !val))) {
     pdg::setLastError("pd_solve_noalloc: null pointer or non-positive vertex count");
     return PD_ERR_INVALID_ARGUMENT;
   }
@@ -83,17 +89,17 @@ extern "C" int pd_solve_noalloc(int32_t n, const int32_t* perm, const int32_t* c
   }
   // Set-up, once per device, with that device current: the array's host-side name is only a
   // stand-in, so the kernel must be given the device address.
-  if (g_scratchAddr[dev] == nullptr) {
-    double* ptr = nullptr;
-    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_noallocScratch);
-    if (e != cudaSuccess || ptr == nullptr) {
+  double* scratch = g_scratchAddr[dev].load(std::memory_order_acquire);
+  if (scratch == nullptr) {
+    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&scratch), g_noallocScratch);
+    if (e != cudaSuccess || scratch == nullptr) {
       pdg::setLastError(std::string("pd_solve_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
       return PD_ERR_CUDA;
     }
-    g_scratchAddr[dev] = ptr;
+    g_scratchAddr[dev].store(scratch, std::memory_order_release);
   }
   solveNoAllocKernel<<<1, 96, 0, static_cast<cudaStream_t>(stream)>>>(n, perm, colptr, rowidx, val, dinv, b, x,
-                                                                       g_scratchAddr[dev]);
+                                                                       scratch);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
     pdg::setLastError(std::string("pd_solve_noalloc: launch failed: ") + cudaGetErrorString(e));

@@ -86,6 +86,40 @@ __global__ void __launch_bounds__(kBlockThreads) solveExactKernel(const Instance
   }
 }
 
+// One column of the solve (IGlobalSolver::solveComponent): the same level schedule and the same
+// per-row order as the three-column solve, so each column's bits equal that column of it.
+__global__ void __launch_bounds__(kBlockThreads) solveColumnExactKernel(const InstanceDev* __restrict__ inst,
+                                                                        const double* __restrict__ b,
+                                                                        double* __restrict__ x,
+                                                                        double* __restrict__ wGlobal, int smemBytes) {
+  extern __shared__ double smem[];
+  const InstanceDev& I = *inst;
+  double* w = (I.n * (int)sizeof(double) <= smemBytes) ? smem : wGlobal;
+  for (int v = threadIdx.x; v < I.n; v += blockDim.x) w[I.iperm[v]] = b[v];
+  __syncthreads();
+  for (int l = 0; l < I.nlevF; ++l) {
+    const int beg = I.fwdPtr[l], end = I.fwdPtr[l + 1];
+    for (int t = beg + threadIdx.x; t < end; t += blockDim.x) {
+      const int r = I.fwdRows[t];
+      double a = w[r];
+      for (int p = I.Lrp[r]; p < I.Lrp[r + 1]; ++p) a = __dsub_rn(a, __dmul_rn(I.Lrv[p], w[I.Lci[p]]));
+      w[r] = a;
+    }
+    __syncthreads();
+  }
+  for (int l = 0; l < I.nlevB; ++l) {
+    const int beg = I.bwdPtr[l], end = I.bwdPtr[l + 1];
+    for (int t = beg + threadIdx.x; t < end; t += blockDim.x) {
+      const int k = I.bwdRows[t];
+      double a = __dmul_rn(w[k], I.dinv[k]);
+      for (int p = I.Lcp[k]; p < I.Lcp[k + 1]; ++p) a = __dsub_rn(a, __dmul_rn(I.Lcv[p], w[I.Lri[p]]));
+      w[k] = a;
+    }
+    __syncthreads();
+  }
+  for (int v = threadIdx.x; v < I.n; v += blockDim.x) x[v] = w[I.iperm[v]];
+}
+
 }  // namespace
 
 int launchSubstepExact(const InstanceDev* d, int count, int substeps, int smemBytes, void* stream, bool timed) {
@@ -100,6 +134,17 @@ int launchSubstepExact(const InstanceDev* d, int count, int substeps, int smemBy
   if (timed) substepExactKernel<true><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   else substepExactKernel<false><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
+}
+
+int launchSolveColumnExact(const InstanceDev* d, const double* b, double* x, double* w, int smemBytes,
+                           void* stream) {
+  // set once, from whichever thread launches first (thread-safe static initialisation): the
+  // three component solves of one solver may be launched from three threads
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(solveColumnExactKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (attr != cudaSuccess) return static_cast<int>(attr);
+  solveColumnExactKernel<<<1, kBlockThreads, smemBytes, static_cast<cudaStream_t>(stream)>>>(d, b, x, w, smemBytes);
+  return static_cast<int>(cudaGetLastError());  // the runtime keeps the last error per host thread
 }
 
 int launchSolveExact(const InstanceDev* d, const double* b, double* x, int smemBytes, void* stream) {

@@ -21,9 +21,35 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["unit"] == "substeps/s" and d["higher_is_better"] is True
     assert d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1 and d["value"] > 0
     assert d["config"]["workload"] == "cloth40_full" and d["config"]["iterations"] == 40
+    assert d["precision"] == "fp64" and d["dtype"] == "f64"
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+
+
+def test_reference_arm_never_loads_the_product():
+    """The reference arm builds its cloths with the oracle alone: after a run, neither the product
+    package nor its library is in the process."""
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '1']; "
+            "bench.main(); maps = open('/proc/self/maps').read(); "
+            "print('PRODUCT', any(m.startswith('pd_gb300') for m in sys.modules), 'libpd_gb300' in maps, "
+            "'libpd_oracle' in maps)")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    last = [ln for ln in r.stdout.splitlines() if ln.startswith("PRODUCT")][-1]
+    assert last == "PRODUCT False False True"
+
+
+def test_both_arms_describe_the_workload_identically(pdg):
+    """`config` is built from the cloths and knobs alone, so the GPU arm (product scenes) and the CPU
+    arms (oracle meshes) print the same dictionary for every workload."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import workloads as OW
+    for name in ("cloth40_plain", "cloth40_full", "cloth256", "batch"):
+        scenes, cfgs, sub = bench.workload(name, 24)
+        meshes, ocfgs, osub = OW.build(name, 24)
+        assert bench.describe_workload(name, scenes, cfgs, sub) == bench.describe_workload(name, meshes, ocfgs, osub)
 
 
 def test_algorithmic_bytes_per_substep():

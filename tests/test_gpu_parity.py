@@ -182,6 +182,55 @@ def test_global_solver_dropin(pdg):
     assert st["analyze_calls"] == 1 and st["factorize_calls"] == 1 and st["solve_calls"] == 1
 
 
+def test_solve_component_from_three_threads(pdg):
+    """The reference's Integrator solves x, y and z from three OpenMP threads at once
+    (core/sim/Integrator.cpp:558-565, IGlobalSolver.h:94-97). Three host threads, each with its own
+    right-hand side, solve their component concurrently 40 times into one shared x; every column
+    must equal that column of a three-column solve of its own b, bit for bit, and no thread may
+    touch another's entries."""
+    import threading
+    scenes, cfg, _ = W.cloth40_full()
+    orc = oracle_twin(scenes[0], cfg)
+    rp, ci, val = orc.matrix()
+    n = scenes[0].n
+    cols, rows, vals = [], [], []
+    for c in range(n):
+        for d in range(3):
+            for p in range(rp[c], rp[c + 1]):
+                rows.append(3 * ci[p] + d)
+                vals.append(val[p])
+            cols.append(len(rows))
+    col_ptr = np.concatenate([[0], np.array(cols)]).astype(np.int32)
+    s = pdg.GpuDirectSolver()
+    s.analyze(3 * n, col_ptr, np.array(rows, np.int32))
+    s.factorize(3 * n, col_ptr, np.array(rows, np.int32), np.array(vals))
+    rng = np.random.default_rng(7)
+    rounds = 40
+    bs = [[rng.standard_normal(3 * n) for _ in range(3)] for _ in range(rounds)]
+    want = [[s.solve(bs[r][c])[c::3].copy() for c in range(3)] for r in range(rounds)]
+    got = [np.full(3 * n, np.nan) for _ in range(rounds)]
+    errors = []
+    start = threading.Barrier(3)
+
+    def worker(c):
+        try:
+            start.wait()
+            for r in range(rounds):
+                s.solve_component(c, bs[r][c], got[r])
+        except Exception as e:  # noqa: BLE001 — reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(c,)) for c in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(120)
+    assert not errors, errors
+    for r in range(rounds):
+        for c in range(3):
+            assert np.array_equal(bits(got[r][c::3]), bits(want[r][c])), (r, c)
+
+
 def test_spring_closed_form_and_equilibrium(pdg):
     """pd_check items 2-5: one-step closed form, equilibrium ℓ − mg/κ, pinned exact, free fall."""
     h, m, ell, k, g = 1.0 / 120.0, 0.05, 0.1, 1.0e4, 9.81
