@@ -639,6 +639,16 @@ def run_ours(args):
     import pd_gb300 as P
 
     scenes, cfgs, sub = workload(args.workload, args.batch_count, args.precision)
+    total_count = len(scenes)
+    described = describe_workload(args.workload, scenes, cfgs, sub)  # the whole workload, every rank's part
+    parts = None
+    if args.workload == "batch" and world > 1:
+        # the batch's cloths split across the ranks (longest processing time first): each rank
+        # steps its part, nothing crosses ranks until the final gather
+        from pd_gb300 import partition as PT
+        parts = PT.partition(PT.scene_costs(scenes, cfgs), world)
+        scenes = [scenes[i] for i in parts[rank]]
+        cfgs = [cfgs[i] for i in parts[rank]]
     sim = P.Simulator(scenes, cfgs)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
@@ -685,6 +695,8 @@ def run_ours(args):
     kernel_ms = ms / args.steps
     count = len(scenes)
     value, t_max = replica_rate(count * args.steps, ms / 1e3, world, "cuda")  # aggregate (cloth-)substeps/s
+    if parts is not None:  # a partitioned batch: every rank's cloths together, over the slowest rank's time
+        value = total_count * args.steps / t_max
 
     # ---- e2e: through the C ABI's host-state call (pd_sim_step_host): every step copies every
     # cloth's positions and velocities in from pinned host memory, runs the substep and copies
@@ -709,7 +721,14 @@ def run_ours(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     h2d = d2h = sum(2 * 24 * sc.n for sc in scenes)
-    e2e_value, _ = replica_rate(count * args.steps, e2e_s, world, "cuda")
+    e2e_value, e2e_max = replica_rate(count * args.steps, e2e_s, world, "cuda")
+    if parts is not None:
+        e2e_value = total_count * args.steps / e2e_max
+    gathered = None
+    if parts is not None:  # the one cross-rank data step: final states to rank 0, after all timing
+        from pd_gb300 import partition as PT
+        states = PT.gather_states(parts, [sim.state(i) for i in range(count)], rank, world)
+        gathered = None if states is None else len(states)
 
     # ---- the plain one-cloth-per-launch FP64 GPU path on the same workload, and the position
     # error of this mode against the FP64 CPU oracle after the workload's full substep count
@@ -733,11 +752,14 @@ def run_ours(args):
         achieved = per_launch_bytes / (kernel_ms * 1e-3) / 1e9
         traffic = profiled_traffic(kernel, args.workload, args.precision)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
+                "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+                "scaling": "strong" if parts is not None else "weak",
                 "vs_baseline": None, "dtype": PRECISIONS[args.precision][1], "data": "synthetic",
-                "config": describe_workload(args.workload, scenes, cfgs, sub),
+                "config": described,
                 "precision": args.precision,
-                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                "parallelism": (f"batch split over {world} ranks, {count} of {total_count} cloths on rank 0, "
+                                f"final states gathered ({gathered})" if parts is not None
+                                else f"replicas x{world}" if world > 1 else "single GPU"),
                 "kernel": {"name": kernel, "ctas_per_cloth": info["cluster_ctas"], "factor_nnz": info["factor_nnz"],
                            "iterations_used_last_timed_substep": iters_used[0]},
                 "wall_s": t_wall,
