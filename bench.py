@@ -55,11 +55,13 @@ def kernel_name(info):
     if kind == 1:
         return "substepGridKernel" if ctas > 16 else "substepClusterKernel" if ctas > 1 else "substepFastKernel"
     if kind == 2:
-        return "substepMixedClusterKernel" if ctas > 1 else "substepMixedKernel"
+        return "substepMixedGridKernel" if ctas > 16 else "substepMixedClusterKernel" if ctas > 1 else "substepMixedKernel"
     if kind == 3:
         return "substepDenseClusterKernel"
     if kind == 4:
         return "substepDeltaKernel"
+    if kind == 6:
+        return "substepDelta64Kernel"
     return "substepCorrGridKernel" if ctas > 16 else "substepCorrClusterKernel" if ctas > 1 else "substepCorrKernel"
 
 
@@ -95,7 +97,7 @@ def parse():
         a.steps = {"differentiable": 3, "batch": 30}.get(a.workload, 600)
     if a.variants is None:
         a.variants = {"cloth40_full": "fp64,fp32-projection,fp32-solve", "cloth40_plain": "fp64,fp32-projection",
-                      "cloth256": "fp64,fp32-projection"}.get(a.workload, "none")
+                      "cloth256": "fp64,fp32-projection,fp32-solve"}.get(a.workload, "none")
     a.variants = [] if a.variants == "none" else [m for m in a.variants.split(",") if m and m != a.precision]
     return a
 

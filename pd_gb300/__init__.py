@@ -23,6 +23,7 @@ from .api import (  # noqa: F401
     PD_SOLVE_DENSE32,
     PD_SOLVE_DENSE32_TEAM,
     PD_SOLVE_SUPERNODAL32_CORRECTION,
+    PD_SOLVE_DENSE64_TEAM,
     PD_HOST_STATE_NONE,
     PD_HOST_STATE_COPIES,
     PD_HOST_STATE_GRAPH,

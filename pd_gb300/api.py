@@ -33,6 +33,7 @@ PD_SOLVE_SUPERNODAL32 = 2
 PD_SOLVE_DENSE32 = 3
 PD_SOLVE_DENSE32_TEAM = 4
 PD_SOLVE_SUPERNODAL32_CORRECTION = 5
+PD_SOLVE_DENSE64_TEAM = 6         # FP64 team kernel: explicit inverse in double-float arithmetic
 PD_HOST_STATE_NONE = 0            # Simulator.info()["host_state"]: no host arrays bound
 PD_HOST_STATE_COPIES = 1          # step_host copies each pageable array with its own copy
 PD_HOST_STATE_GRAPH = 2           # step_host: gather/scatter kernels in one CUDA graph

@@ -24,7 +24,9 @@ UNITS = {
     "substep_exact.cu": ["-fmad=false"],
     "substep_fast.cu": [],
     "substep_mixed.cu": [],
+    "substep_mixed_grid.cu": [],
     "substep_delta.cu": [],
+    "substep_delta64.cu": [],
     "substep_corr.cu": [],
     "adjoint.cu": [],
     "solve_noalloc.cu": ["-fmad=false"],

@@ -95,7 +95,7 @@ struct Instance {
   size_t oX, oV, oXn, oXhat, oXsol, oBbase, oM, oPin, oQ, oBend, oEab, oRest, oK, oKd, oRc, oSs, oSi, oRs, oRi, oBs,
       oBi, oBf, oBabc, oIperm, oLrp, oLci, oLrv, oLcp, oLri, oLcv, oDinv, oFp, oFr, oBp, oBr, oW, oLastRes,
       oEarly, oIters, oConv, oLvlPtr, oLvlRows, oRowSn, oSnStart, oOffEnd, oOffBeg, oSnInv, oInvL, oInvLT, oT,
-      oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv,
+      oLvlG, oLvlG32, oLrv32, oLcv32, oInvL32, oInvLT32, oDinv32, oAptr, oAcol, oAval, oX0, oY32, oT32, oAinv, oAinvLo,
       oVptr, oVcol, oVval, oRtag, oXtag, oPtag, oEpoch, oWindow, oErr, oTEdge, oTBend, oTVtx, oQhl, oXhl,
       oXhatHl, oD, oCscToCsr, oAPosCsc, oAPosDiag, oSnByLevel;
   bool gpuRefactor = false;   // the next upload computes the factor's values on the device
@@ -255,8 +255,28 @@ int deltaSmem(const Instance& I, int team, int* resRows) {
   return static_cast<int>(fixed + 4L * rows * ld);
 }
 
+// Shared memory of the FP64 team kernel for one instance (pdg::Delta64Carve), with as many resident
+// rows of Ã⁻¹ (hi and lo, 8 bytes an entry) as fit in kDeltaSmem: all of the CTA's rows, else a
+// multiple of four.
+int delta64Smem(const Instance& I, int team, int* resRows) {
+  const int n = I.scene.n, ld = (n + 31) / 32 * 32, chunk = (n + team - 1) / team;
+  int eCap = 0, bCap = 0;
+  teamCaps(I, team, &eCap, &bCap);
+  const int wCap = teamWindowCap(I, team);
+  const long fixed = static_cast<long>(pdg::Delta64Carve(n, ld, 0, wCap, eCap, bCap, chunk).total);
+  long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (8L * ld) : 0;
+  if (rows >= chunk) {
+    rows = chunk;
+  } else {
+    rows &= ~3L;  // whole groups of four rows
+  }
+  *resRows = static_cast<int>(rows);
+  return static_cast<int>(pdg::Delta64Carve(n, ld, static_cast<int>(rows), wCap, eCap, bCap, chunk).total);
+}
+
 // kind: 0 none, 1 dense inverse (cluster kernel), 2 dense inverse + team kernel buffers,
-// 3 FP32 tables + position pairs of the one-CTA correction kernel
+// 3 FP32 tables + position pairs of the one-CTA correction kernel, 4 dense inverse as hi/lo pairs +
+// FP64 team kernel buffers
 void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencyScale = 1.0) {
   const auto& s = I.scene;
   const size_t n = s.n, ne = s.edges.size(), nb = s.bends.size();
@@ -264,30 +284,33 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencySc
   const size_t before = A.host.size();
   I.denseLd = 0;
   I.denseResRows = 0;
-  I.oAinv = I.oVptr = I.oVcol = I.oVval = 0;
+  I.oAinv = I.oAinvLo = I.oVptr = I.oVcol = I.oVval = 0;
   I.oRtag = I.oXtag = I.oPtag = I.oEpoch = I.oWindow = I.oErr = I.oTEdge = I.oTBend = I.oTVtx = I.oQhl = 0;
   I.oXhl = I.oXhatHl = 0;
   I.teamECap = I.teamBCap = I.teamWCap = 0;
-  if (denseKind == 1 || denseKind == 2) {
+  if (denseKind == 1 || denseKind == 2 || denseKind == 4) {
     // Ã⁻¹ (FP32, rows padded to 32) is filled on the GPU after the upload (launchDenseInverse)
     I.denseLd = static_cast<int>((n + 31) / 32 * 32);
     I.oAinv = A.zeros(4 * n * static_cast<size_t>(I.denseLd));
+    if (denseKind == 4) I.oAinvLo = A.zeros(4 * n * static_cast<size_t>(I.denseLd));
     I.oVptr = A.add(I.L.rowptr);
     I.oVcol = A.add(I.L.col);
     I.oVval = A.add(I.L.val);
   }
-  if (denseKind == 2) {
-    deltaSmem(I, teamCtas, &I.denseResRows);
+  if (denseKind == 2 || denseKind == 4) {
+    if (denseKind == 2) deltaSmem(I, teamCtas, &I.denseResRows);
+    else delta64Smem(I, teamCtas, &I.denseResRows);
     teamCaps(I, teamCtas, &I.teamECap, &I.teamBCap);
     I.teamWCap = teamWindowCap(I, teamCtas);
-    I.oRtag = A.zeros(8 * 2 * 3 * n);  // two buffers
-    I.oXtag = A.zeros(8 * 6 * n);
+    // two buffers of 3n values: one word each (FP32), two words each (FP64)
+    I.oRtag = A.zeros(8 * 2 * 3 * n * (denseKind == 4 ? 2 : 1));
+    I.oXtag = A.zeros(8 * 6 * n);  // 3n positions: hi and lo (FP32), or low and high words (FP64)
     I.oPtag = A.zeros(8 * 3 * 16 * static_cast<size_t>(teamCtas));  // A (two buffers), B; a line each
     I.oEpoch = A.zeros(4);
     I.oErr = A.zeros(4);
     I.oWindow = A.add(teamWindows(I, teamCtas));
   }
-  if (denseKind >= 2) {
+  if (denseKind == 2 || denseKind == 3) {
     // incidences in the kernels' FP32 form (pinned endpoints flagged in bit 31)
     auto bitsOf = [](float f) {
       int32_t i;
@@ -395,10 +418,12 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencySc
   I.oInvLT = A.add(I.F.invLT);
   I.oT = A.zeros(24 * n);
   // FP32 solve: the correction kernel's teams are 256-thread CTAs, the other mixed kernels' 1024
-  I.oLvlG32 = A.add(denseKind == 3 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam, latencyScale)
-                                   : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
-                                                                                : pdg::kBlockThreads,
-                                                              1, latencyScale));
+  // (a grid team, teamCtas > 16: rows strided over all of its 256-thread CTAs)
+  I.oLvlG32 = A.add(denseKind == 3  ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam, latencyScale)
+                    : teamCtas > 16 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, teamCtas, latencyScale)
+                                    : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
+                                                                                 : pdg::kBlockThreads,
+                                                               1, latencyScale));
   I.oLrv32 = A.add(I.F.rowval32);
   I.oLcv32 = A.add(I.F.colval32);
   I.oInvL32 = A.add(I.F.invL32);
@@ -552,6 +577,7 @@ pdg::InstanceDev describe(const Instance& I, uint8_t* base, int32_t* iterLog, ui
   d.denseLd = I.denseLd;
   if (I.denseLd > 0) {
     d.Ainv = reinterpret_cast<const float*>(P(I.oAinv));
+    d.AinvLo = I.oAinvLo ? reinterpret_cast<const float*>(P(I.oAinvLo)) : nullptr;
     d.Vptr = reinterpret_cast<const int32_t*>(P(I.oVptr));
     d.Vcol = reinterpret_cast<const int32_t*>(P(I.oVcol));
     d.Vval = reinterpret_cast<const double*>(P(I.oVval));
@@ -622,6 +648,7 @@ struct pd_sim {
   int teamCtas = 1;  // CTAs per instance (a thread-block cluster when > 1)
   bool dense = false;  // mixed modes: the cluster applies the explicit FP32 inverse
   bool delta = false;  // MIXED: a team of co-resident CTAs per cloth, correction-form dense solve
+  bool delta64 = false;  // FP64: the same team form, FP64 correction and double-float Ã⁻¹ product
   bool corr = false;   // MIXED above the dense limit: one CTA per cloth, correction-form FP32 solve
   int corrBig = 0;     // batch: instances (first in dDescOrder) run by clusters of kBatchCluster CTAs
   cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
@@ -678,8 +705,10 @@ struct pd_sim {
     teamCtas = 1;
     dense = false;
     delta = false;
+    delta64 = false;
     corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
+    if (p == PD_PRECISION_FP64 && planDelta64()) return;
     for (auto& I : inst) I.corrTeam = 1;
     corrBig = 0;
     if (p == PD_PRECISION_MIXED) {
@@ -726,6 +755,22 @@ struct pd_sim {
         return;
       }
       want = 16;
+    }
+    // FP32 solve of one cloth above the explicit-inverse limit: a grid team too (each CTA of a
+    // cluster would hold the whole system in its shared memory, which a large cloth does not fit)
+    if (p == PD_PRECISION_FP32_SOLVE && inst.size() == 1 && inst[0].scene.n > denseLimit() &&
+        pdg::mixedGridCapacity() > 16) {
+      if (inst[0].cfg.cluster_ctas <= 0 && plan.team_ctas <= 0 && inst[0].scene.n >= kBatchClusterMinVertices &&
+          pdg::mixedGridCapacity() > 32)
+        want = pdg::mixedGridCapacity() / 2;
+      if (want > 16) {  // its team-maximum slots (2 per CTA) live in the 3n-double workspace x0
+        const int ctas = std::min({want, pdg::mixedGridCapacity(), 3 * inst[0].scene.n / 2});
+        if (ctas > 16) {
+          teamCtas = ctas;
+          return;
+        }
+        want = 16;
+      }
     }
     int cs = 1;
     while (cs * 2 <= std::min(want, 16)) cs *= 2;
@@ -774,6 +819,36 @@ struct pd_sim {
     if (pdg::deltaResidentCtas(smem) < count * team) return false;
     teamCtas = team;
     delta = true;
+    return true;
+  }
+  // FP64 with every cloth small enough for the explicit inverse and no over-relaxation: a team of
+  // co-resident CTAs per cloth (the SMs shared out over the cloths, or a requested team of more than
+  // 16 CTAs); a requested cluster of 1–16 CTAs keeps the supernodal kernel.
+  bool planDelta64() {
+    int maxN = 0, minN = 1 << 30;
+    for (const auto& I : inst) {
+      if (I.cfg.cheb_mode != PD_CHEB_OFF) return false;
+      maxN = std::max(maxN, I.scene.n);
+      minN = std::min(minN, I.scene.n);
+    }
+    if (maxN > denseLimit()) return false;
+    const int want = wantCtas();
+    if (want > 0 && want <= 16) return false;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const int count = static_cast<int>(inst.size());
+    int team = want > 0 ? want : sms / count;
+    team = std::min({team, sms / count, minN, 256});  // 256: partials one polling warp covers
+    if (team < 2) return false;
+    int smem = 0, rows = 0;
+    for (const auto& I : inst) smem = std::max(smem, delta64Smem(I, team, &rows));
+    if (pdg::delta64ResidentCtas(smem) < count * team) return false;
+    teamCtas = team;
+    delta64 = true;
     return true;
   }
   // CTAs per cloth of the correction kernel: a cluster for a few large cloths (as for the FP64
@@ -833,7 +908,7 @@ struct pd_sim {
   int upload(int capacity) {
     Arena A;
     planTeam();
-    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : corr ? 3 : dense ? 1 : 0, latencyScale());
+    for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : delta64 ? 4 : corr ? 3 : dense ? 1 : 0, latencyScale());
     release();
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
@@ -988,14 +1063,15 @@ struct pd_sim {
                               stageTiming ? dStage + pdg::kStageCount * i : nullptr));
       // exact: one 3n workspace; fast: two (RHS / solution and the level temporaries)
       int rows = 0;
-      const int need = delta   ? deltaSmem(inst[i], teamCtas, &rows)
+      const int need = delta     ? deltaSmem(inst[i], teamCtas, &rows)
+                       : delta64 ? delta64Smem(inst[i], teamCtas, &rows)
                        : dense ? denseSmem(inst[i].scene.n)
                        : corr  ? 24 * inst[i].scene.n
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       // the correction kernel keeps its solve vectors in shared memory up to 48 KB, so that a
       // batch still runs four CTAs per SM
       const int cap = corr ? ((teamCtas > 1 || inst[i].corrTeam > 1) ? 0 : 48 * 1024) : kMaxSmem;
-      if ((delta || need <= cap) && need > smem) smem = need;
+      if ((delta || delta64 || need <= cap) && need > smem) smem = need;
     }
     smemBytes = smem;
     if (!dDesc) PD_CUDA(cudaMalloc(&dDesc, sizeof(pdg::InstanceDev) * inst.size()));
@@ -1028,7 +1104,7 @@ struct pd_sim {
   // barrier counters are reset so that later launches start clean).
   int sync() {
     PD_CUDA(cudaStreamSynchronize(stream));
-    if (!delta) return PD_OK;
+    if (!delta && !delta64) return PD_OK;
     int bad = 0;
     for (const auto& I : inst) {
       int32_t e = 0;
@@ -1040,7 +1116,7 @@ struct pd_sim {
       PD_CUDA(cudaMemset(dArena + I.oErr, 0, 4));
       PD_CUDA(cudaMemset(dArena + I.oEpoch, 0, 4));
       PD_CUDA(cudaMemset(dArena + I.oPtag, 0, 8 * 3 * 16 * static_cast<size_t>(teamCtas)));
-      PD_CUDA(cudaMemset(dArena + I.oRtag, 0, 8 * 2 * 3 * static_cast<size_t>(I.scene.n)));
+      PD_CUDA(cudaMemset(dArena + I.oRtag, 0, 8 * 2 * 3 * static_cast<size_t>(I.scene.n) * (delta64 ? 2 : 1)));
       PD_CUDA(cudaMemset(dArena + I.oXtag, 0, 8 * 6 * static_cast<size_t>(I.scene.n)));
     }
     return fail(PD_ERR_CUDA, "a team exchange of the substep kernel gave up waiting; the state is undefined");
@@ -1076,6 +1152,8 @@ struct pd_sim {
       rc = pdg::launchSubstepExact(dDesc, count, substeps, smemBytes, st, stageTiming);
     } else if (delta) {
       rc = pdg::launchSubstepDelta(dDesc, count, teamCtas, smemBytes, substeps, st, stageTiming);
+    } else if (delta64) {
+      rc = pdg::launchSubstepDelta64(dDesc, count, teamCtas, smemBytes, substeps, st, stageTiming);
     } else if (corr) {
       if (teamCtas > 16) {  // one cloth on a cooperative grid of CTAs
         rc = pdg::launchSubstepCorrGrid(dDesc, teamCtas, substeps, st, stageTiming);
@@ -1103,8 +1181,9 @@ struct pd_sim {
     } else if (dense) {
       rc = pdg::launchSubstepDenseCluster(dDesc, count, teamCtas, smemBytes, substeps, st);
     } else if (mixedSolve(p)) {
-      rc = teamCtas > 1 ? pdg::launchSubstepMixedCluster(dDesc, count, teamCtas, smemBytes, substeps, st)
-                        : pdg::launchSubstepMixed(dDesc, count, substeps, smemBytes, st);
+      rc = teamCtas > 16  ? pdg::launchSubstepMixedGrid(dDesc, teamCtas, substeps, st, stageTiming)
+           : teamCtas > 1 ? pdg::launchSubstepMixedCluster(dDesc, count, teamCtas, smemBytes, substeps, st)
+                          : pdg::launchSubstepMixed(dDesc, count, substeps, smemBytes, st);
     } else {
       rc = teamCtas > 16  ? pdg::launchSubstepGrid(dDesc, teamCtas, substeps, st, stageTiming)
            : teamCtas > 1 ? pdg::launchSubstepCluster(dDesc, count, teamCtas, substeps, st, stageTiming)
@@ -1588,7 +1667,8 @@ int pd_sim_step_host(pd_sim* s, int32_t substeps) {
     for (size_t i = 0; i < count; ++i) {
       s->hostTable[i].dx = reinterpret_cast<double*>(s->dArena + s->inst[i].oX);
       s->hostTable[i].dv = reinterpret_cast<double*>(s->dArena + s->inst[i].oV);
-      s->hostTable[i].err = s->delta ? reinterpret_cast<const int32_t*>(s->dArena + s->inst[i].oErr) : nullptr;
+      s->hostTable[i].err = (s->delta || s->delta64) ? reinterpret_cast<const int32_t*>(s->dArena + s->inst[i].oErr)
+                                                      : nullptr;
     }
     if (!s->dHostTable) PD_CUDA(cudaMalloc(&s->dHostTable, sizeof(pdg::HostStateDev) * count));
     PD_CUDA(cudaMemcpy(s->dHostTable, s->hostTable.data(), sizeof(pdg::HostStateDev) * count,
@@ -1787,6 +1867,7 @@ int pd_sim_get_info(pd_sim* s, int32_t i, pd_sim_info* out) {
                                                                                  : PD_HOST_STATE_GRAPH;
   const int p = s->precision();
   out->solve_kind = p == PD_PRECISION_FP64_EXACT ? PD_SOLVE_LEVELS
+                    : s->delta64                 ? PD_SOLVE_DENSE64_TEAM
                     : !mixedSolve(p)             ? PD_SOLVE_SUPERNODAL
                     : s->delta                   ? PD_SOLVE_DENSE32_TEAM
                     : s->corr                    ? PD_SOLVE_SUPERNODAL32_CORRECTION
@@ -1989,7 +2070,7 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
   const int count = static_cast<int>(s->inst.size());
   if (rc == PD_OK && p != PD_PRECISION_FP64_EXACT) {
     const int team0 = s->teamCtas;
-    const bool delta = s->delta, corr = s->corr, supernodal = !s->delta && !s->dense;
+    const bool delta = s->delta || s->delta64, corr = s->corr, supernodal = !delta && !s->dense;
     if (delta) {  // team sizes below the built-in SMs ÷ cloths
       for (int t : {team0 * 3 / 4, team0 / 2, team0 / 4})
         if (t >= 2 && t != team0) {
@@ -2009,8 +2090,9 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
         }
     } else {  // CTAs per cloth of the cluster kernels; one large MIXED cloth also on a grid of CTAs
       std::vector<int> sizes = count <= 9 ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{1, 2, 4};
-      if ((corr || supernodalFp64(p)) && count == 1) {
-        const int cap = corr ? pdg::corrGridCapacity() : pdg::gridCapacity();
+      const bool mixedGrid = p == PD_PRECISION_FP32_SOLVE && count == 1 && s->inst[0].scene.n > s->denseLimit();
+      if ((corr || supernodalFp64(p) || mixedGrid) && count == 1) {
+        const int cap = corr ? pdg::corrGridCapacity() : mixedGrid ? pdg::mixedGridCapacity() : pdg::gridCapacity();
         for (int g : {cap / 4, cap / 2, cap})
           if (g > 16) sizes.push_back(g);
       }

@@ -97,6 +97,8 @@ struct InstanceDev {
   // Ã in vertex order (FP64) for the refinement residual
   int32_t denseLd;
   const float* Ainv;
+  const float* AinvLo;         // FP64 team kernel: Ã⁻¹ − Ainv as FP32 (Ainv + AinvLo = the FP64 inverse
+                               // to ≈2⁻⁴⁸ relative), rows padded to denseLd; null otherwise
   const int32_t* Vptr;
   const int32_t* Vcol;
   const double* Vval;
@@ -204,6 +206,11 @@ int clusterSizeSupported(int want);
 // cooperative launch (the cluster code with grid barriers); gridCapacity: the most CTAs it holds.
 int launchSubstepGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
 int gridCapacity();
+// FP32-solve substep (FP32 supernodal solve + one FP64 refinement step) of one large cloth on a
+// cooperative grid of `ctas` 256-thread CTAs (substep_mixed_grid.cu); mixedGridCapacity() is the
+// most CTAs co-resident on the device.
+int launchSubstepMixedGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
+int mixedGridCapacity();
 // Mixed-precision substep (FP32 solve + one FP64 refinement step): one CTA per instance with
 // smemBytes of workspace (72·n when it fits, else 0 = global), or a cluster of clusterSize CTAs
 // per instance, each CTA solving the whole system in its own shared memory (72·max n bytes).
@@ -236,6 +243,56 @@ int corrClusterSupported(int cs);
 int launchSubstepCorrGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
 int corrGridCapacity();
 constexpr int kDeltaThreads = 512;
+
+// FP64 team kernel (substep_delta64.cu) on `team` CTAs of kDeltaThreads threads per cloth, the
+// correction form with Ã⁻¹·r in double-float arithmetic; delta64ResidentCtas as deltaResidentCtas.
+int launchSubstepDelta64(const InstanceDev* dInstances, int count, int team, int smemBytes, int substeps,
+                         void* stream, bool timed = false);
+int delta64ResidentCtas(int smemBytes);
+
+// Column segments a row group of Ã⁻¹ is split into by the FP64 team kernel (its partial sums of Δ).
+constexpr int kDelta64Segments = 2;
+
+// Byte offsets of the FP64 team kernel's dynamic shared memory, computed alike on the host (to size
+// the launch and the rows of Ã⁻¹ that fit) and in the kernel. FP32 arrays first (16-byte aligned
+// float4 rows: ld is a multiple of 32), then FP64, then int32:
+//   r as hi and lo (3·ld floats each), resident rows of Ã⁻¹ as hi and lo (resRows·ld each),
+//   window positions (3·wCap), per own edge incidence ℓ, κ and per bend incidence (−k)·w_v,
+//   per own vertex m/h², m, x̂, x_n, v and the segments' partial sums of Δ,
+//   per edge incidence the other vertex, per bend incidence its three vertices, per own vertex
+//   the pinned flag, and the incidence offsets of own vertices.
+struct Delta64Carve {
+  size_t rh, rl, ah, al, xw, erest, ekap, bfac, mh2, mass, xh, xn, v, dl, eo, bv, pin, eb, bb, total;
+  __host__ __device__ Delta64Carve(int n, int ld, int resRows, int wCap, int eCap, int bCap, int chunk) {
+    (void)n;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t at = o;
+      o += bytes;
+      return at;
+    };
+    rh = take(12ull * ld);
+    rl = take(12ull * ld);
+    ah = take(4ull * resRows * ld);
+    al = take(4ull * resRows * ld);
+    xw = take(24ull * wCap);
+    erest = take(8ull * eCap);
+    ekap = take(8ull * eCap);
+    bfac = take(8ull * bCap);
+    mh2 = take(8ull * chunk);
+    mass = take(8ull * chunk);
+    xh = take(24ull * chunk);
+    xn = take(24ull * chunk);
+    v = take(24ull * chunk);
+    dl = take(24ull * kDelta64Segments * chunk);
+    eo = take(4ull * eCap);
+    bv = take(12ull * bCap);
+    pin = take(4ull * chunk);
+    eb = take(4ull * (chunk + 1));
+    bb = take(4ull * (chunk + 1));
+    total = o;
+  }
+};
 
 // Work arrays of one gradient problem (adjoint.cu): the loss is the mean over free vertices of
 // |x_S − target|² after S substeps with the iteration count fixed.

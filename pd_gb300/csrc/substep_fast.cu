@@ -96,9 +96,16 @@ __global__ void __launch_bounds__(kBlockThreads) denseInverseKernel(const Instan
   const Team<false> tm{0, 1};
   TeamSolve<false>::run(I, tm, w, t);
   float* A = const_cast<float*>(I.Ainv);
+  float* Alo = const_cast<float*>(I.AinvLo);  // the FP64 team kernel also keeps the FP32 remainder
   for (int c = 0; c < 3 && v0 + c < n; ++c) {
     float* row = A + static_cast<size_t>(v0 + c) * I.denseLd;
-    for (int u = threadIdx.x; u < n; u += blockDim.x) row[u] = static_cast<float>(w[3 * I.iperm[u] + c]);
+    float* rowLo = Alo ? Alo + static_cast<size_t>(v0 + c) * I.denseLd : nullptr;
+    for (int u = threadIdx.x; u < n; u += blockDim.x) {
+      const double a = w[3 * I.iperm[u] + c];
+      const float hi = static_cast<float>(a);
+      row[u] = hi;
+      if (rowLo) rowLo[u] = static_cast<float>(a - static_cast<double>(hi));
+    }
   }
 }
 

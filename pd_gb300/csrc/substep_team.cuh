@@ -339,8 +339,10 @@ struct TeamSolve {
 };
 
 // Whole substeps of one instance by a team (same steps and formulas as runSubsteps in
-// substep_common.cuh, with FMA contraction allowed).
-template <bool CLUSTER, bool TIMED = false>
+// substep_common.cuh, with FMA contraction allowed). Solve::run(I, tm, w, t) turns the gathered
+// right-hand side in w (elimination order) into the solution, with t a second 3n workspace: the
+// FP64 supernodal solve, or the FP32 solve with one FP64 refinement step (substep_mixed_grid.cu).
+template <bool CLUSTER, bool TIMED = false, class Solve = TeamSolve<CLUSTER>>
 __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, int substeps, double* w, double* t,
                                 double* red, double* slots) {
   int parity = 0;
@@ -374,7 +376,7 @@ __device__ void runSubstepsTeam(const InstanceDev& I, const Team<CLUSTER>& tm, i
       for (int v = T; v < I.n; v += NT) gatherRow(I, tm, v, w);
       tm.sync();
       clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageScatter);
-      TeamSolve<CLUSTER>::run(I, tm, w, t);
+      Solve::run(I, tm, w, t);
       clk.lap(I, tm.rank == 0 && threadIdx.x == 0, kStageSolve);
       // unpack + displacement scan; an over-relaxed iteration puts x_prev + (x_solve − x_prev)·ω
       // and keeps x_solve for the residual (Integrator.cpp:631-641)

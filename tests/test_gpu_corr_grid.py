@@ -88,6 +88,7 @@ def test_grid_team_is_capped_by_its_slot_workspace(pdg):
     for (nx, ny), cap in (((8, 6), 72), ((3, 3), 16)):
         cfg = copy.copy(W._base(grid_nx=nx, grid_ny=ny, grid_spacing=0.05, max_iterations=4))
         cfg.precision = 1
+        cfg.dense_max_vertices = -1  # the supernodal kernel (small FP64 cloths otherwise take the team kernel)
         scene = pdg.make_grid(cfg)
         sim = pdg.Simulator(scene, cfg)
         sim.set_plan({"team_ctas": 300})
@@ -96,3 +97,23 @@ def test_grid_team_is_capped_by_its_slot_workspace(pdg):
         sim.step(3)
         orc.step(3)
         assert max_rel(sim.state()[0], orc.state()[0]) <= 1e-10
+
+
+@pytest.mark.parametrize("gate", ["residual", "displacement"])
+def test_fp32_solve_grid_team_matches_oracle(pdg, gate):
+    """FP32 solve + one FP64 refinement step of one cloth above the explicit-inverse limit on a grid
+    team (the planner's choice for a large cloth), against the oracle."""
+    kw = {"residual": {}, "displacement": {"residual_tolerance": 0.0, "rel_tolerance": 1e-3}}[gate]
+    cfg = copy.copy(W._base(grid_nx=96, grid_ny=90, grid_spacing=1 / 95, max_iterations=12, shear_stiffness=900.0,
+                            bend_stiffness=40.0, **kw))
+    cfg.precision = 3
+    scene = pdg.make_grid(cfg)
+    sim = pdg.Simulator(scene, cfg)
+    info = sim.info()
+    assert info["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32 and info["cluster_ctas"] > 16
+    orc = oracle_twin(scene, cfg, perm=sim.factor()["perm"])
+    for _ in range(3):  # repeated launches: the grid barrier state carries over
+        sim.step(8)
+    its_o, _ = orc.step(24)
+    assert max_rel(sim.state()[0], orc.state()[0]) <= 1e-5
+    assert np.mean(sim.iteration_log()[0] == its_o[-8:]) >= 0.9

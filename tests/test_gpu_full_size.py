@@ -1,8 +1,9 @@
 """The benchmark workloads at their full sizes against the FP64 CPU oracle, run as the bench runs them.
 
 * cloth256: one 256 × 256 cloth (65,536 vertices, 195,585 distance + shear edges, 130,048 bend
-  stencils), 20 iterations, 300 substeps: MIXED (correction form on a grid team of CTAs) and FP32
-  projection within 1e-5 of the oracle after all 300 substeps, FP64 within 1e-10.
+  stencils), 20 iterations, 300 substeps: MIXED (correction form), FP32 projection and FP32 solve +
+  one FP64 refinement step, each on a grid team of CTAs, within 1e-5 of the oracle after all 300
+  substeps; FP64 within 1e-10.
 * batch: the 512 cloths of 16²–128² in one launch, MIXED, 300 substeps: the 16 largest cloths and 16
   more drawn with a fixed seed, each within 1e-5 of its own oracle run.
 * differentiable: the 64 × 64 cloth over 120 substeps (10 iterations each): loss and gradients of the
@@ -49,7 +50,7 @@ def _run(pdg, ref, precision, substeps):
     return sim
 
 
-@pytest.mark.parametrize("precision", [4, 2])
+@pytest.mark.parametrize("precision", [4, 2, 3])
 def test_cloth256_reduced_precision_300_substeps(pdg, cloth256_oracle, precision):
     ref = cloth256_oracle
     sim = _run(pdg, ref, precision, ref["S"])
@@ -140,3 +141,47 @@ def test_differentiable_64x64_gradient_matches_cpu_adjoint(pdg):
     for key in ("dkappa", "dv0", "dforce"):
         rel = np.linalg.norm(g[key] - r[key]) / np.linalg.norm(r[key])
         assert rel < 1e-8, (key, rel)
+
+
+def test_differentiable_64x64_richardson_differences(pdg):
+    """Directional derivatives of the adjoint against Richardson-extrapolated central differences of
+    the GPU loss, R(ε) = (4·D(ε/2) − D(ε))/3 at ε = 2e-5 (the O(ε²) term of D cancels, so a step
+    large enough to clear the FP64 loss's rounding noise keeps a small truncation error), on 16
+    directions drawn as the bench draws them (σ = 100 in scaled units: κ relative to itself, v₀ in
+    m/s, the force in vertex weights). Bars: the median direction within 1e-7 relative, at least 15
+    of the 16 within 1e-6, every one within 1e-8 of its scale ‖g‖·‖d‖ (a direction whose
+    derivative nearly cancels resolves no better than that), and the norm-wise error within 1e-7."""
+    scene, cfg, S, kstar = W.differentiable()
+    c = copy.copy(cfg)
+    c.precision = 1
+    twin = oracle_twin(scene, c, threads=os.cpu_count() or 1)
+    twin.set_edge_stiffness(kstar)
+    twin.step(S)
+    target = twin.state()[0]
+    zero = np.zeros((scene.n, 3))
+    g = pdg.Simulator(scene, c).gradient(S, target, zero)
+    rng = np.random.default_rng(2)
+    k0 = np.asarray(scene.edge_stiffness, np.float64)
+    weight = np.asarray(scene.masses, np.float64)[:, None] * 9.81
+    dirs = [(k0 * rng.normal(0.0, 100.0, k0.shape), rng.normal(0.0, 100.0, (scene.n, 3)),
+             weight * rng.normal(0.0, 100.0, (scene.n, 3))) for _ in range(16)]
+    adj = np.array([g["dkappa"] @ dk + np.sum(g["dv0"] * dv) + np.sum(g["dforce"] * df) for dk, dv, df in dirs])
+    scale = np.array([np.linalg.norm(g["dkappa"]) * np.linalg.norm(dk) + np.linalg.norm(g["dv0"]) * np.linalg.norm(dv)
+                      + np.linalg.norm(g["dforce"]) * np.linalg.norm(df) for dk, dv, df in dirs])
+    fd_sim = pdg.Simulator([scene] * 32, [c] * 32)
+    D = {}
+    for eps in (2e-5, 1e-5):
+        forces = []
+        for j, (dk, dv, df) in enumerate(dirs):
+            for s, sign in enumerate((1.0, -1.0)):
+                fd_sim.set_edge_stiffness(k0 + sign * eps * dk, 2 * j + s)
+                fd_sim.set_state(2 * j + s, scene.positions, sign * eps * dv)
+                forces.append(sign * eps * df)
+        losses = fd_sim.gradient(S, [target] * 32, forces, grad=False)
+        D[eps] = np.array([(losses[2 * j]["loss"] - losses[2 * j + 1]["loss"]) / (2 * eps) for j in range(16)])
+    R = (4.0 * D[1e-5] - D[2e-5]) / 3.0
+    rel = np.abs(R - adj) / np.abs(adj)
+    assert np.median(rel) <= 1e-7, rel
+    assert np.sum(rel <= 1e-6) >= 15, rel
+    assert np.max(np.abs(R - adj) / scale) <= 1e-8
+    assert np.linalg.norm(R - adj) / np.linalg.norm(adj) <= 1e-7
