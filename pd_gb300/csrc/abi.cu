@@ -2073,7 +2073,13 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
     const bool delta = s->delta || s->delta64, corr = s->corr, supernodal = !delta && !s->dense;
     if (delta) {  // team sizes below the built-in SMs ÷ cloths
       for (int t : {team0 * 3 / 4, team0 / 2, team0 / 4})
-        if (t >= 2 && t != team0) {
+        if (t >= 2 && t != team0 && (!s->delta64 || t > 16)) {
+          pd_plan c = start;
+          c.team_ctas = t;
+          run(c);
+        }
+      if (s->delta64)  // and the FP64 supernodal kernel on one CTA or a 16-CTA cluster per cloth
+        for (int t : {1, 16}) {
           pd_plan c = start;
           c.team_ctas = t;
           run(c);

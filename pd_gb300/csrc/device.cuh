@@ -258,11 +258,13 @@ constexpr int kDelta64Segments = 2;
 // float4 rows: ld is a multiple of 32), then FP64, then int32:
 //   r as hi and lo (3·ld floats each), resident rows of Ã⁻¹ as hi and lo (resRows·ld each),
 //   window positions (3·wCap), per own edge incidence ℓ, κ and per bend incidence (−k)·w_v,
-//   per own vertex m/h², m, x̂, x_n, v and the segments' partial sums of Δ,
+//   per own vertex m/h², m, x̂, x_n, v and t (the residual force), per edge and per bend incidence
+//   its six FP64 terms, the segments' partial sums of Δ as FP32 pairs,
 //   per edge incidence the other vertex, per bend incidence its three vertices, per own vertex
-//   the pinned flag, and the incidence offsets of own vertices.
+//   the pinned flag, the incidence offsets of own vertices, and each incidence's own vertex.
 struct Delta64Carve {
-  size_t rh, rl, ah, al, xw, erest, ekap, bfac, mh2, mass, xh, xn, v, dl, eo, bv, pin, eb, bb, total;
+  size_t rh, rl, ah, al, xw, erest, ekap, bfac, mh2, mass, xh, xn, v, tres, econ, bcon, dl, eo, bv, pin, eb, bb,
+      eown, bown, total;
   __host__ __device__ Delta64Carve(int n, int ld, int resRows, int wCap, int eCap, int bCap, int chunk) {
     (void)n;
     size_t o = 0;
@@ -284,12 +286,17 @@ struct Delta64Carve {
     xh = take(24ull * chunk);
     xn = take(24ull * chunk);
     v = take(24ull * chunk);
-    dl = take(24ull * kDelta64Segments * chunk);
+    tres = take(24ull * chunk);
+    econ = take(48ull * eCap);
+    bcon = take(48ull * bCap);
+    dl = take(24ull * kDelta64Segments * chunk);  // 2 floats for each of 3·chunk entries per segment
     eo = take(4ull * eCap);
     bv = take(12ull * bCap);
     pin = take(4ull * chunk);
     eb = take(4ull * (chunk + 1));
     bb = take(4ull * (chunk + 1));
+    eown = take(4ull * eCap);
+    bown = take(4ull * bCap);
     total = o;
   }
 };

@@ -35,7 +35,6 @@ namespace pdg {
 namespace {
 
 constexpr int kWarps = kDeltaThreads / 32;
-constexpr int kGroup = 16;                  // lanes per vertex in the correction pass
 constexpr long long kSpinLimit = 1ll << 22; // poll rounds before an exchange gives up
 constexpr int kMaxTeam = 256;               // partials one polling warp covers (kMaxTeam / 32 a lane)
 constexpr int kSegments = kDelta64Segments; // most column segments a row group of Ã⁻¹ is split into
@@ -59,9 +58,9 @@ __device__ __forceinline__ void publish(unsigned long long* p, unsigned tag, dou
   storeRelaxed(p + 1, t | static_cast<unsigned>(__double2hiint(v)));
 }
 
-// Polls the FP64 values [b, e) of src (value j in words 2j, 2j + 1) until both words of each carry
-// `tag`, and hands each to sink(j, value); thread `tid` of `nth` takes every nth value, B values in
-// flight. False if a word stayed stale for kSpinLimit rounds.
+// Polls the values [b, e) of src (value j in words 2j, 2j + 1) until both words of each carry `tag`,
+// and hands each to sink(j, low 32 bits of word 2j, of word 2j + 1); thread `tid` of `nth` takes every
+// nth value, B values in flight. False if a word stayed stale for kSpinLimit rounds.
 template <int B, class Sink>
 __device__ __forceinline__ bool pollValues(const unsigned long long* src, int b, int e, unsigned tag, int tid,
                                            int nth, Sink&& sink) {
@@ -98,21 +97,25 @@ __device__ __forceinline__ bool pollValues(const unsigned long long* src, int b,
     }
 #pragma unroll
     for (int u = 0; u < B; ++u)
-      if (j0 + u * nth < e) sink(j0 + u * nth, __hiloint2double(static_cast<int>(hi[u]), static_cast<int>(lo[u])));
+      if (j0 + u * nth < e) sink(j0 + u * nth, lo[u], hi[u]);
   }
   return true;
 }
 
-__device__ __forceinline__ double warpMaxD(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
+// Non-negative doubles order like their bit patterns read as signed 64-bit integers, so their maxima
+// are taken with integer operations: on this part an FP64 warp instruction occupies its sub-core's
+// FP64 pipe for ~80 cycles whatever its active lanes, and these reductions would otherwise be a
+// large share of an iteration. A NaN counts as 0 (it is skipped, as the reference's `>` skips it).
+__device__ __forceinline__ long long maxKey(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? 0ll : b;
 }
 
-__device__ __forceinline__ double warpSumD(double v) {
+__device__ __forceinline__ double warpMaxNonNeg(double v) {
+  long long b = maxKey(v);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  return __longlong_as_double(b);
 }
 
 // Warp 0: maximum of the FP64 partials tagged `tag` of the team's ranks into *out (words 0 and 1 of
@@ -151,19 +154,15 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
     __nanosleep(nap);
     nap = min(2 * nap, 256u);
   }
-  double mx = 0.0;
+  long long mx = 0;
 #pragma unroll
   for (int i = 0; i < kMaxTeam / 32; ++i)
-    if (lane + 32 * i < team) mx = fmax(mx, __hiloint2double(static_cast<int>(hi[i]), static_cast<int>(lo[i])));
-  mx = warpMaxD(mx);
-  if (lane == 0) *out = mx;
+    if (lane + 32 * i < team)
+      mx = max(mx, maxKey(__hiloint2double(static_cast<int>(hi[i]), static_cast<int>(lo[i]))));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) *out = __longlong_as_double(mx);
   return good;
-}
-
-// FP64 value as an FP32 pair with hi + lo = v to ~2⁻⁴⁸ relative.
-__device__ __forceinline__ void splitF(double v, float& hi, float& lo) {
-  hi = __double2float_rn(v);
-  lo = __double2float_rn(v - static_cast<double>(hi));
 }
 
 // (s, c) += (ah + al)·(rh + rl) as double-float: ah·rh = p + e exactly (FMA), s + p = t + err exactly
@@ -180,12 +179,22 @@ __device__ __forceinline__ void dfTerm(float& s, float& c, float ah, float al, f
   c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(e, x)));
 }
 
+// (s, c) + (s2, c2) for double-float pairs: the two-sum of s and s2, the rest into c.
+__device__ __forceinline__ void dfAdd(float& s, float& c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float bb = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(c2, err));
+}
+
 // Up to NR rows of Ã⁻¹ (hi rows from Ah0, lo rows from Al0, nr of them) times the three components
 // of r (hi in Rh, lo in Rl, component-major with row length ld) over the float4 columns [jb, je),
-// one warp; each r load serves NR rows. Sums (FP64) land in dl[3·(li + r) + c].
+// one warp; each r load serves NR rows. The lanes' double-float sums are reduced over the warp in
+// FP32 and land as a pair, dh[3·(li + r) + c] + dlo[3·(li + r) + c].
 template <int NR, bool SMEM>
 __device__ __forceinline__ void rowGroup(const float* Ah0, const float* Al0, int nr, const float* Rh,
-                                         const float* Rl, int ld, int li, int jb, int je, double* dl) {
+                                         const float* Rl, int ld, int li, int jb, int je, float* dh, float* dlo) {
   const int lane = threadIdx.x & 31;
   const float4* ah4 = reinterpret_cast<const float4*>(Ah0);
   const float4* al4 = reinterpret_cast<const float4*>(Al0);
@@ -221,101 +230,72 @@ __device__ __forceinline__ void rowGroup(const float* Ah0, const float* Al0, int
   for (int r = 0; r < NR; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const double v = warpSumD(static_cast<double>(s[r][c]) + static_cast<double>(cc[r][c]));
-      if (lane == 0 && r < nr) dl[3 * (li + r) + c] = v;
+      float hs = s[r][c], hc = cc[r][c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        dfAdd(hs, hc, __shfl_xor_sync(0xffffffffu, hs, o), __shfl_xor_sync(0xffffffffu, hc, o));
+      if (lane == 0 && r < nr) {
+        dh[3 * (li + r) + c] = hs;
+        dlo[3 * (li + r) + c] = hc;
+      }
     }
 }
 
-// Incidence sums of one vertex in FP64, accumulated by the lanes of a group and then reduced (the
-// FP64 form of correction.cuh's CorrectionSums).
-struct CorrectionSums64 {
-  double a[3] = {0.0, 0.0, 0.0};  // mass + edge terms of t
-  double f[3] = {0.0, 0.0, 0.0};  // bend terms of t
-  double p[3] = {0.0, 0.0, 0.0};  // what the matrix adds to f − a by seeing pinned vertices at q
+// ℓ/‖rel‖ for dot = rel·rel > 0: the FP32 reciprocal square root refined by two Newton steps in FP64
+// (2⁻²² → 2⁻⁴⁴ → FP64 rounding), fewer FP64 instructions than a square root and a division.
+__device__ __forceinline__ double restOverLength(double dot, double rest) {
+  double y = static_cast<double>(rsqrtf(static_cast<float>(dot)));
+  const double nh = -0.5 * dot;
+  y = y * fma(nh * y, y, 1.5);
+  y = y * fma(nh * y, y, 1.5);
+  return rest * y;
+}
 
-  // Edge incidences [e0, e1) (other vertex | pinned << 31, ℓ, κ) and bend incidences [s0, s1)
-  // (a, b, c each | pinned << 31, (−k)·w_v); lane gl of G takes every G-th. Xw holds the window's
-  // positions (vertex u at 3·(u − wlo)).
-  __device__ __forceinline__ void accumulate(const InstanceDev& I, const int* eo, const double* erest,
-                                             const double* ekap, int e0, int e1, const int* bv, const double* bf,
-                                             int s0, int s1, const double* Xw, int wlo, const double* xv, int gl,
-                                             int G) {
-    for (int q = e0 + gl; q < e1; q += G) {
-      const int oo = eo[q];
-      const int o = oo & 0x7fffffff;
-      const double* xo = Xw + 3 * (o - wlo);
-      const double rx = xv[0] - xo[0], ry = xv[1] - xo[1], rz = xv[2] - xo[2];  // x_v − x_o
-      const double len = sqrt(rx * rx + ry * ry + rz * rz);
-      double dx = 0.0, dy = 0.0, dz = 0.0;
-      if (!(len <= 1e-12)) {
-        const double sc = erest[q] / len;
-        dx = rx * sc;
-        dy = ry * sc;
-        dz = rz * sc;
-      }
-      const double kap = ekap[q];
-      a[0] = fma(kap, rx - dx, a[0]);
-      a[1] = fma(kap, ry - dy, a[1]);
-      a[2] = fma(kap, rz - dz, a[2]);
-      if (oo < 0) {  // pinned neighbour: the matrix sees it at q
-        const double qx = __ldg(I.q + 3 * o), qy = __ldg(I.q + 3 * o + 1), qz = __ldg(I.q + 3 * o + 2);
-        p[0] = fma(kap, (xv[0] - qx) - rx, p[0]);
-        p[1] = fma(kap, (xv[1] - qy) - ry, p[1]);
-        p[2] = fma(kap, (xv[2] - qz) - rz, p[2]);
-      }
+// The terms of one edge incidence of own vertex v (other vertex o, FP64): κ·((x_v − x_o) − d_e) into
+// t[0..2] and, when o is pinned, what the matrix adds by seeing o at q, κ·((x_v − q_o) − (x_v − x_o)),
+// into t[3..5] (zeros otherwise). d_e = ℓ·rel/‖rel‖, zero when ‖rel‖ ≤ 1e-12 (DistanceTerm.cpp:94-102).
+__device__ __forceinline__ void edgeIncidence(const InstanceDev& I, const double* xv, const double* xo, int oo,
+                                              double rest, double kap, double* t) {
+  const double rx = xv[0] - xo[0], ry = xv[1] - xo[1], rz = xv[2] - xo[2];
+  const double dot = fma(rx, rx, fma(ry, ry, rz * rz));
+  double sc = 0.0;
+  if (!(dot <= 1e-24)) sc = restOverLength(dot, rest);
+  t[0] = kap * (rx - rx * sc);
+  t[1] = kap * (ry - ry * sc);
+  t[2] = kap * (rz - rz * sc);
+  if (oo < 0) {
+    const int o = oo & 0x7fffffff;
+    t[3] = kap * ((xv[0] - __ldg(I.q + 3 * o)) - rx);
+    t[4] = kap * ((xv[1] - __ldg(I.q + 3 * o + 1)) - ry);
+    t[5] = kap * ((xv[2] - __ldg(I.q + 3 * o + 2)) - rz);
+  } else {
+    t[3] = t[4] = t[5] = 0.0;
+  }
+}
+
+// The terms of one bend incidence (members a, b, c with pinned flags, fac = (−k)·w_v): fac·(w·x)
+// into t[0..2] and, with pinned members, fac·(w·x − w·x̃) with x̃ = q on pinned members into t[3..5].
+__device__ __forceinline__ void bendIncidence(const InstanceDev& I, const double* Xw, int wlo, const int* mb,
+                                              double fac, double* t) {
+  const int ia = mb[0] & 0x7fffffff, ib = mb[1] & 0x7fffffff, ic = mb[2] & 0x7fffffff;
+  const double* xa = Xw + 3 * (ia - wlo);
+  const double* xb = Xw + 3 * (ib - wlo);
+  const double* xc = Xw + 3 * (ic - wlo);
+  const bool pinnedAny = (mb[0] | mb[1] | mb[2]) < 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double s3 = (xa[c] - xb[c]) + (xc[c] - xb[c]);
+    t[c] = fac * s3;
+    double pc = 0.0;
+    if (pinnedAny) {
+      const double ya = mb[0] < 0 ? __ldg(I.q + 3 * ia + c) : xa[c];
+      const double yb = mb[1] < 0 ? __ldg(I.q + 3 * ib + c) : xb[c];
+      const double yc = mb[2] < 0 ? __ldg(I.q + 3 * ic + c) : xc[c];
+      pc = fac * (s3 - ((ya - yb) + (yc - yb)));
     }
-    for (int q = s0 + gl; q < s1; q += G) {
-      const int ma = bv[3 * q], mb = bv[3 * q + 1], mc = bv[3 * q + 2];
-      const int ia = ma & 0x7fffffff, ib = mb & 0x7fffffff, ic = mc & 0x7fffffff;
-      const double fac = bf[q];
-      const double* xa = Xw + 3 * (ia - wlo);
-      const double* xb = Xw + 3 * (ib - wlo);
-      const double* xc = Xw + 3 * (ic - wlo);
-      double s3[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        s3[c] = (xa[c] - xb[c]) + (xc[c] - xb[c]);
-        f[c] = fma(fac, s3[c], f[c]);
-      }
-      if ((ma | mb | mc) < 0) {  // pinned members: the matrix part sees them at q
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const double ya = ma < 0 ? __ldg(I.q + 3 * ia + c) : xa[c];
-          const double yb = mb < 0 ? __ldg(I.q + 3 * ib + c) : xb[c];
-          const double yc = mc < 0 ? __ldg(I.q + 3 * ic + c) : xc[c];
-          p[c] = fma(fac, s3[c] - ((ya - yb) + (yc - yb)), p[c]);
-        }
-      }
-    }
+    t[3 + c] = pc;
   }
-  // mass term (x − x̂)·m/h², added by one lane
-  __device__ __forceinline__ void addMass(const double* xv, const double* xh, double mh2) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) a[c] = fma(xv[c] - xh[c], mh2, a[c]);
-  }
-  template <int G>
-  __device__ __forceinline__ void reduce() {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) {
-        a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
-        f[c] += __shfl_xor_sync(0xffffffffu, f[c], o);
-        p[c] += __shfl_xor_sync(0xffffffffu, p[c], o);
-      }
-    }
-  }
-  // ‖t‖ / m (Integrator.cpp:230-263)
-  __device__ __forceinline__ double residual(double mass) const {
-    const double t0 = a[0] + f[0], t1 = a[1] + f[1], t2 = a[2] + f[2];
-    return sqrt(t0 * t0 + t1 * t1 + t2 * t2) / mass;
-  }
-  // r = −(mass + edge terms) + bend terms, pinned neighbours at q
-  __device__ __forceinline__ void correction(double* r) const {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) r[c] = (f[c] - a[c]) - p[c];
-  }
-};
+}
 
 template <bool TIMED>
 __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const InstanceDev* __restrict__ insts,
@@ -345,7 +325,13 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
   double* xh64 = reinterpret_cast<double*>(smem + cv.xh);
   double* xn64 = reinterpret_cast<double*>(smem + cv.xn);
   double* v64 = reinterpret_cast<double*>(smem + cv.v);
-  double* dl = reinterpret_cast<double*>(smem + cv.dl);  // kSegments × 3·chunk
+  float* dh = reinterpret_cast<float*>(smem + cv.dl);  // kSegments × 3·chunk: Δ per segment, hi
+  float* dlo = dh + kSegments * 3 * chunk;              // and lo
+  double* econ = reinterpret_cast<double*>(smem + cv.econ);  // 6 per edge incidence
+  double* bcon = reinterpret_cast<double*>(smem + cv.bcon);  // 6 per bend incidence
+  double* tres = reinterpret_cast<double*>(smem + cv.tres);  // t of own vertices (3 per vertex)
+  int* eOwn = reinterpret_cast<int*>(smem + cv.eown);        // own vertex (local index) of each incidence
+  int* bOwn = reinterpret_cast<int*>(smem + cv.bown);
   int* eo = reinterpret_cast<int*>(smem + cv.eo);
   int* bv = reinterpret_cast<int*>(smem + cv.bv);
   int* pinnedOwn = reinterpret_cast<int*>(smem + cv.pin);
@@ -380,6 +366,10 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
     sEb[t] = (m > 0) ? I.rstart[rb + t] - e0 : 0;
     sBb[t] = (m > 0) ? I.bstart[rb + t] - b0 : 0;
   }
+  for (int li = threadIdx.x; li < m; li += blockDim.x) {
+    for (int q = I.rstart[rb + li] - e0; q < I.rstart[rb + li + 1] - e0; ++q) eOwn[q] = li;
+    for (int q = I.bstart[rb + li] - b0; q < I.bstart[rb + li + 1] - b0; ++q) bOwn[q] = li;
+  }
   for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) v64[t] = I.v[3 * rb + t];
   for (int t = threadIdx.x; t < 3 * (whi - wlo); t += blockDim.x) Xw[t] = I.x[3 * wlo + t];
   for (int j = n + threadIdx.x; j < ld; j += blockDim.x)
@@ -400,7 +390,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
   const int groups = (m + kGroupRows - 1) / kGroupRows;
   const int segs = groups > 0 ? max(1, min(kSegments, kWarps / groups)) : 1;
   const int q4 = ld / 4;
-  const int gl = threadIdx.x & (kGroup - 1), group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
+  const int ePad = (eN + 31) & ~31;  // edge incidences in the first warps, bend incidences after them
   __syncthreads();
 
   const StageClock<TIMED> clk(I, rank == 0 && threadIdx.x == 0);
@@ -415,7 +405,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
       xh64[t] = xh;
       sc = fmax(sc, fabs(xh - p));
     }
-    const double scW = warpMaxD(sc);
+    const double scW = warpMaxNonNeg(sc);
     __syncthreads();  // x̂ of own rows is read by other threads below
     clk.lap(I, rank == 0 && threadIdx.x == 0, kStagePredict);
     double scale = 0.0;
@@ -427,53 +417,77 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
       const unsigned buf = (tagA >> 1) & 1u;
       unsigned long long* rtag = I.rtag + static_cast<size_t>(buf) * 6 * n;
       unsigned long long* ptagA = I.ptag + buf * kPartStride * team;
-      // correction r and residual of x^k for own vertices, kGroup lanes per vertex (FP64)
-      double resLocal = 0.0;
-      for (int base = 0; base < m; base += ngroups) {
-        const int li = base + group;
-        const bool active = li < m;
-        const bool isFree = active && pinnedOwn[li] == 0;
-        const int v = rb + li;
-        CorrectionSums64 cs;
-        if (isFree) {
-          const double* xv = Xw + 3 * (v - wlo);
-          cs.accumulate(I, eo, erest, ekap, sEb[li], sEb[li + 1], bv, bfac, sBb[li], sBb[li + 1], Xw, wlo, xv, gl,
-                        kGroup);
-          if (gl == 0) cs.addMass(xv, xh64 + 3 * li, mh2[li]);
+      // correction r and residual of x^k for own vertices (FP64; Integrator.cpp:230-263 for the
+      // residual): one lane per incidence computes its terms, then three lanes per vertex sum them in
+      // incidence order, then one lane per vertex takes the residual's norm. r is published as FP32
+      // hi/lo words, the pair the product needs.
+      for (int t = threadIdx.x; t < ePad + bN; t += blockDim.x) {
+        if (t < eN) {
+          const int li = eOwn[t];
+          const double* xv = Xw + 3 * (rb + li - wlo);
+          const double* xo = Xw + 3 * ((eo[t] & 0x7fffffff) - wlo);
+          edgeIncidence(I, xv, xo, eo[t], erest[t], ekap[t], econ + 6 * t);
+        } else if (t >= ePad) {
+          const int q = t - ePad;
+          bendIncidence(I, Xw, wlo, bv + 3 * q, bfac[q], bcon + 6 * q);
         }
-        cs.reduce<kGroup>();
-        if (active && gl == 0) {
-          double r[3] = {0.0, 0.0, 0.0};
-          if (isFree) {
-            if (mass[li] > 0.0) resLocal = fmax(resLocal, cs.residual(mass[li]));
-            cs.correction(r);
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < 3 * m; t += blockDim.x) {
+        const int li = t / 3, c = t - 3 * li, v = rb + li;
+        double r = 0.0, tv = 0.0;
+        if (!pinnedOwn[li]) {
+          double a = 0.0, f = 0.0, pc = 0.0;
+          for (int q = sEb[li]; q < sEb[li + 1]; ++q) {
+            a += econ[6 * q + c];
+            pc += econ[6 * q + 3 + c];
           }
-          for (int c = 0; c < 3; ++c) publish(rtag + 2 * (3 * static_cast<size_t>(v) + c), tagA, r[c]);
+          for (int q = sBb[li]; q < sBb[li + 1]; ++q) {
+            f += bcon[6 * q + c];
+            pc += bcon[6 * q + 3 + c];
+          }
+          a = fma(Xw[3 * (v - wlo) + c] - xh64[t], mh2[li], a);  // mass term (x − x̂)·m/h²
+          tv = a + f;
+          r = (f - a) - pc;
         }
+        tres[t] = tv;
+        const float hi = __double2float_rn(r);
+        const float lo = __double2float_rn(r - static_cast<double>(hi));
+        unsigned long long* w = rtag + 2 * (3 * static_cast<size_t>(v) + c);
+        const unsigned long long tg = static_cast<unsigned long long>(tagA) << 32;
+        storeRelaxed(w, tg | __float_as_uint(hi));
+        storeRelaxed(w + 1, tg | __float_as_uint(lo));
+      }
+      __syncthreads();
+      double resLocal = 0.0;
+      for (int li = threadIdx.x; li < m; li += blockDim.x) {
+        if (pinnedOwn[li] || !(mass[li] > 0.0)) continue;
+        const double t0 = tres[3 * li], t1 = tres[3 * li + 1], t2 = tres[3 * li + 2];
+        resLocal = fmax(resLocal, sqrt(fma(t0, t0, fma(t1, t1, t2 * t2))) / mass[li]);
       }
       // exchange A, a full barrier of the team: the whole correction (warps 1..) and the maximum
       // of the residuals — at k = 0 of the scale — (warp 0)
-      resLocal = warpMaxD(resLocal);
+      resLocal = warpMaxNonNeg(resLocal);
       if (lane == 0) red[warp] = (k == 0) ? scW : resLocal;
       __syncthreads();
       clk.lap(I, rank == 0 && threadIdx.x == 0, kStageLocal);  // the correction pass: projection, scatter and residual in one
       bool ok = true;
       if (warp == 0) {
         if (lane == 0) {
-          double pm = 0.0;
-          for (int w = 0; w < kWarps; ++w) pm = fmax(pm, red[w]);
-          if (!(I.withholdRank == rank && step == 0 && k == 0)) publish(ptagA + kPartStride * rank, tagA, pm);
+          long long pm = 0;
+          for (int w = 0; w < kWarps; ++w) pm = max(pm, maxKey(red[w]));
+          if (!(I.withholdRank == rank && step == 0 && k == 0))
+            publish(ptagA + kPartStride * rank, tagA, __longlong_as_double(pm));
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
       } else {
-        ok = pollValues<5>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32, [&](int j, double val) {
-          const int v = j / 3, c = j - 3 * v;
-          float hi, lo;
-          splitF(val, hi, lo);
-          Rh[c * ld + v] = hi;
-          Rl[c * ld + v] = lo;
-        });
+        ok = pollValues<5>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32,
+                           [&](int j, unsigned wh, unsigned wl) {  // r as its FP32 pair
+                             const int v = j / 3, c = j - 3 * v;
+                             Rh[c * ld + v] = __uint_as_float(wh);
+                             Rl[c * ld + v] = __uint_as_float(wl);
+                           });
       }
       if (!ok) failed = 1;
       __syncthreads();
@@ -498,13 +512,15 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
         const int li = kGroupRows * (task / segs), sg = task - (task / segs) * segs;
         const int jb = q4 * sg / segs, je = q4 * (sg + 1) / segs;
         const int nr = min(kGroupRows, m - li);
-        double* out = dl + sg * 3 * chunk;
+        float* oh = dh + sg * 3 * chunk;
+        float* ol = dlo + sg * 3 * chunk;
         if (li < resRows) {  // resRows is a multiple of 4 unless it covers every row
           rowGroup<kGroupRows, true>(Ah + static_cast<size_t>(li) * ld, Al + static_cast<size_t>(li) * ld, nr, Rh,
-                                     Rl, ld, li, jb, je, out);
+                                     Rl, ld, li, jb, je, oh, ol);
         } else {
           rowGroup<kGroupRows, false>(I.Ainv + static_cast<size_t>(rb + li) * ld,
-                                      I.AinvLo + static_cast<size_t>(rb + li) * ld, nr, Rh, Rl, ld, li, jb, je, out);
+                                      I.AinvLo + static_cast<size_t>(rb + li) * ld, nr, Rh, Rl, ld, li, jb, je, oh,
+                                      ol);
         }
       }
       __syncthreads();
@@ -521,8 +537,9 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
           dmax = fmax(dmax, fabs(qv - x));
           x = qv;
         } else {
-          double d = dl[t];
-          for (int sgi = 1; sgi < segs; ++sgi) d += dl[sgi * 3 * chunk + t];
+          float hs = dh[t], hc = dlo[t];  // the segments' pairs summed in FP32, then one FP64 sum
+          for (int sgi = 1; sgi < segs; ++sgi) dfAdd(hs, hc, dh[sgi * 3 * chunk + t], dlo[sgi * 3 * chunk + t]);
+          const double d = static_cast<double>(hs) + static_cast<double>(hc);
           dmax = fmax(dmax, fabs(d));
           x += d;
         }
@@ -533,16 +550,18 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
       // the displacements (warp 0), which makes it a full barrier — with the residual gate a CTA
       // waits only for the CTAs owning its window
       __syncthreads();  // own positions are read back by other threads below
-      auto sinkX = [&](int j, double val) { Xw[j - 3 * wlo] = val; };
+      auto sinkX = [&](int j, unsigned wl, unsigned wh) {  // a position: low and high words of the FP64
+        Xw[j - 3 * wlo] = __hiloint2double(static_cast<int>(wh), static_cast<int>(wl));
+      };
       if (!I.useResidual) {
-        dmax = warpMaxD(dmax);
+        dmax = warpMaxNonNeg(dmax);
         if (lane == 0) red[warp] = dmax;
         __syncthreads();
         if (warp == 0) {
           if (lane == 0) {
-            double pm = 0.0;
-            for (int w = 0; w < kWarps; ++w) pm = fmax(pm, red[w]);
-            publish(ptagB + kPartStride * rank, tagB, pm);
+            long long pm = 0;
+            for (int w = 0; w < kWarps; ++w) pm = max(pm, maxKey(red[w]));
+            publish(ptagB + kPartStride * rank, tagB, __longlong_as_double(pm));
           }
           __syncwarp();
           ok = pollPartials(ptagB, team, tagB, &gate);
