@@ -322,6 +322,11 @@ typedef struct pd_plan {
                                 this many vertices run as clusters on a second stream (built-in
                                 8192; < 0: none) */
   int32_t big_cluster_ctas;  /* CTAs of each of those clusters (built-in 4) */
+  int32_t work_threads;      /* MIXED batches above the explicit-inverse limit: 256 = one 256-thread
+                                CTA per cloth, all launched at once (with the large cloths on
+                                clusters as above; built-in); 512 or 1024 = the batch as a work table:
+                                resident CTAs of this many threads take the cloths largest first from
+                                a counter until none is left (no clusters) */
   double latency_scale;      /* weight of the dependent-latency term against the issue term in the
                                 lanes-per-row model of every supernodal level (built-in 1) */
 } pd_plan;

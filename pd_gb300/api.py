@@ -93,7 +93,7 @@ class _SimInfo(C.Structure):
 
 class _Plan(C.Structure):
     _fields_ = [("team_ctas", C.c_int32), ("big_min_vertices", C.c_int32), ("big_cluster_ctas", C.c_int32),
-                ("latency_scale", C.c_double)]
+                ("work_threads", C.c_int32), ("latency_scale", C.c_double)]
 
 
 PD_TUNE_MAX_CANDIDATES = 32

@@ -104,6 +104,7 @@ struct Instance {
   std::vector<int32_t> patRowptr, patCol;  // pattern of Ã the current symbolic factor was built for
   int denseLd = 0;      // > 0: Ã⁻¹ is in the arena
   int corrTeam = 1;     // correction kernel: CTAs (a cluster when > 1) running this instance
+  int corrThreads = pdg::kBlockThreads;  // correction kernel: threads of the CTA(s) running it
   int denseResRows = 0; // team kernel: rows of Ã⁻¹ each CTA keeps in shared memory
   int teamECap = 0, teamBCap = 0;
   int teamWCap = 0;     // most window vertices of one CTA
@@ -419,7 +420,7 @@ void layout(Instance& I, Arena& A, int teamCtas, int denseKind, double latencySc
   I.oT = A.zeros(24 * n);
   // FP32 solve: the correction kernel's teams are 256-thread CTAs, the other mixed kernels' 1024
   // (a grid team, teamCtas > 16: rows strided over all of its 256-thread CTAs)
-  I.oLvlG32 = A.add(denseKind == 3  ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, I.corrTeam, latencyScale)
+  I.oLvlG32 = A.add(denseKind == 3  ? pdg::chooseGroupWidths32(I.F, I.corrThreads, I.corrTeam, latencyScale)
                     : teamCtas > 16 ? pdg::chooseGroupWidths32(I.F, pdg::kBlockThreads, teamCtas, latencyScale)
                                     : pdg::chooseGroupWidths32(I.F, teamCtas > 1 ? pdg::kClusterThreads
                                                                                  : pdg::kBlockThreads,
@@ -651,6 +652,8 @@ struct pd_sim {
   bool delta64 = false;  // FP64: the same team form, FP64 correction and double-float Ã⁻¹ product
   bool corr = false;   // MIXED above the dense limit: one CTA per cloth, correction-form FP32 solve
   int corrBig = 0;     // batch: instances (first in dDescOrder) run by clusters of kBatchCluster CTAs
+  int workThreads = 0; // batch: > 0 runs it as a work table on resident CTAs of this many threads
+  int* dCounter = nullptr;  // the work table's next-cloth counter
   cudaStream_t aux = nullptr;   // second stream: the batch's large cloths beside the small ones
   cudaEvent_t forkEv = nullptr, joinEv = nullptr;
   unsigned generation = 0;      // bumped whenever the arena, the descriptors or the plan change
@@ -680,6 +683,7 @@ struct pd_sim {
     if (hStatus) cudaFreeHost(hStatus);
     if (dStage) cudaFree(dStage);
     if (ownStream) cudaStreamDestroy(ownStream);
+    if (dCounter) cudaFree(dCounter);
   }
   void dropGraph() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
@@ -709,14 +713,22 @@ struct pd_sim {
     corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
     if (p == PD_PRECISION_FP64 && planDelta64()) return;
-    for (auto& I : inst) I.corrTeam = 1;
+    for (auto& I : inst) {
+      I.corrTeam = 1;
+      I.corrThreads = pdg::kBlockThreads;
+    }
     corrBig = 0;
+    workThreads = 0;
     if (p == PD_PRECISION_MIXED) {
       if (!planDelta()) {
         corr = true;
         teamCtas = planCorr();
         if (teamCtas > 1) {
           for (auto& I : inst) I.corrTeam = teamCtas;
+        } else if (inst.size() > 1 && plan.work_threads > pdg::kBlockThreads) {
+          // the batch as a work table on resident CTAs of work_threads threads (no clusters)
+          workThreads = plan.work_threads;
+          for (auto& I : inst) I.corrThreads = workThreads;
         } else if (inst.size() > 1 && plan.big_min_vertices >= 0 &&
                    pdg::corrClusterSupported(bigCs = plan.big_cluster_ctas > 0 ? plan.big_cluster_ctas
                                                                                : kBatchCluster) == bigCs) {
@@ -910,6 +922,7 @@ struct pd_sim {
     planTeam();
     for (auto& I : inst) layout(I, A, teamCtas, delta ? 2 : delta64 ? 4 : corr ? 3 : dense ? 1 : 0, latencyScale());
     release();
+    if (workThreads > 0 && !dCounter) PD_CUDA(cudaMalloc(&dCounter, sizeof(int)));  // before any capture
     PD_CUDA(cudaMalloc(&dArena, A.host.size()));
     arenaBytes = A.host.size();
     PD_CUDA(cudaMemcpy(dArena, A.host.data(), A.host.size(), cudaMemcpyHostToDevice));
@@ -1070,7 +1083,11 @@ struct pd_sim {
                                : workspaceBytesPerVertex(precision()) * inst[i].scene.n;
       // the correction kernel keeps its solve vectors in shared memory up to 48 KB, so that a
       // batch still runs four CTAs per SM
-      const int cap = corr ? ((teamCtas > 1 || inst[i].corrTeam > 1) ? 0 : 48 * 1024) : kMaxSmem;
+      const int cap = corr ? ((teamCtas > 1 || inst[i].corrTeam > 1) ? 0
+                              : workThreads >= 1024       ? kMaxSmem       // one CTA an SM
+                              : workThreads > 0           ? 100 * 1024     // two CTAs an SM
+                                                          : 48 * 1024)
+                           : kMaxSmem;
       if ((delta || delta64 || need <= cap) && need > smem) smem = need;
     }
     smemBytes = smem;
@@ -1159,6 +1176,9 @@ struct pd_sim {
         rc = pdg::launchSubstepCorrGrid(dDesc, teamCtas, substeps, st, stageTiming);
       } else if (teamCtas > 1) {
         rc = pdg::launchSubstepCorrCluster(dDesc, count, teamCtas, substeps, st, stageTiming);
+      } else if (workThreads > 0) {
+        rc = pdg::launchSubstepCorrWork(dDescOrder ? dDescOrder : dDesc, count, dCounter, workThreads, substeps,
+                                        smemBytes, st, stageTiming);
       } else if (corrBig > 0) {
         // the one-CTA launch of the smaller cloths on this stream, submitted first, then the large
         // cloths' clusters on the second stream behind an event wait: the one-CTA cloths take
@@ -1991,6 +2011,8 @@ static pd_plan effectivePlan(const pd_sim* s) {
   p.team_ctas = s->teamCtas;
   p.big_min_vertices = s->plan.big_min_vertices != 0 ? s->plan.big_min_vertices : kBatchClusterMinVertices;
   p.big_cluster_ctas = s->bigCs;
+  p.work_threads = (s->corr && s->teamCtas == 1 && s->inst.size() > 1)
+                       ? (s->workThreads > 0 ? s->workThreads : pdg::kBlockThreads) : 0;
   p.latency_scale = s->latencyScale();
   return p;
 }
@@ -2011,7 +2033,8 @@ static int timeSubsteps(pd_sim* s, int substeps, cudaEvent_t e0, cudaEvent_t e1,
 static bool validPlan(const pd_plan& p) {
   return p.team_ctas >= 0 && p.team_ctas <= 1024 && (p.big_cluster_ctas == 0 || (p.big_cluster_ctas >= 2 &&
          p.big_cluster_ctas <= 16)) && std::isfinite(p.latency_scale) && p.latency_scale >= 0.0 &&
-         p.latency_scale <= 1e3;
+         p.latency_scale <= 1e3 &&
+         (p.work_threads == 0 || p.work_threads == 256 || p.work_threads == 512 || p.work_threads == 1024);
 }
 
 int pd_sim_set_plan(pd_sim* s, const pd_plan* plan) {
@@ -2091,9 +2114,18 @@ int pd_sim_autotune(pd_sim* s, int32_t substeps, pd_plan* tried, double* ms_per_
           pd_plan c = start;
           c.big_min_vertices = minN;
           c.big_cluster_ctas = cs;
-          if (minN == effective[0].big_min_vertices && cs == effective[0].big_cluster_ctas) continue;
+          if (minN == effective[0].big_min_vertices && cs == effective[0].big_cluster_ctas &&
+              effective[0].work_threads == pdg::kBlockThreads)
+            continue;
+          c.work_threads = pdg::kBlockThreads;
           run(c);
         }
+      for (int wt : {512, 1024}) {  // the batch as a work table
+        pd_plan c = start;
+        c.work_threads = wt;
+        if (wt == effective[0].work_threads) continue;
+        run(c);
+      }
     } else {  // CTAs per cloth of the cluster kernels; one large MIXED cloth also on a grid of CTAs
       std::vector<int> sizes = count <= 9 ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{1, 2, 4};
       const bool mixedGrid = p == PD_PRECISION_FP32_SOLVE && count == 1 && s->inst[0].scene.n > s->denseLimit();

@@ -241,6 +241,11 @@ int corrClusterSupported(int cs);
 // One cloth (dInstances[0]) by `ctas` co-resident CTAs on a cooperative launch: the cluster code
 // with grid barriers. corrGridCapacity: the most CTAs such a launch can hold on this device.
 int launchSubstepCorrGrid(const InstanceDev* dInstances, int ctas, int substeps, void* stream, bool timed = false);
+// A MIXED batch above the explicit-inverse limit as a work table (substep_corr.cu): resident CTAs of
+// `threads` (512 or 1024) threads take cloths in descriptor order from *counter (reset here, on the
+// stream, before the launch) until none is left; dynamic shared memory smemBytes per CTA.
+int launchSubstepCorrWork(const InstanceDev* dInstances, int count, int* counter, int threads, int substeps,
+                          int smemBytes, void* stream, bool timed = false);
 int corrGridCapacity();
 constexpr int kDeltaThreads = 512;
 

@@ -235,6 +235,36 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const 
   runSubstepsCorr<true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
+// A batch as a work table: resident CTAs of WT threads each take the next cloth from an integer
+// counter (the descriptors come largest first), run all of its substeps, and take another until the
+// table is empty. A cloth is run by exactly one CTA, so its bits do not depend on which CTA takes it
+// or when; the counter is the only shared word (integer atomics, no waiting on other CTAs). Against
+// one 256-thread CTA per cloth all launched at once, a CTA has four times the threads to hide the
+// solve's load latency, and no SM idles while another finishes a large cloth.
+template <int WT, bool TIMED>
+__global__ void __launch_bounds__(WT, 1024 / WT) substepCorrWorkKernel(const InstanceDev* __restrict__ insts,
+                                                                       int count, int* counter, int substeps,
+                                                                       int smemBytes) {
+  extern __shared__ float sm[];
+  __shared__ double red[32];
+  __shared__ double slots[2];
+  __shared__ int taken;
+  for (;;) {
+    if (threadIdx.x == 0) taken = atomicAdd(counter, 1);
+    __syncthreads();
+    const int idx = taken;
+    __syncthreads();  // every thread has read `taken` before thread 0 takes the next cloth
+    if (idx >= count) break;
+    const InstanceDev& I = insts[idx];
+    const bool inSmem = 24 * I.n <= smemBytes;  // Y, T: 3n floats each
+    float* Y = inSmem ? sm : I.y32;
+    float* T = inSmem ? sm + 3 * I.n : I.t32;
+    const Team<false> tm{0, 1};
+    runSubstepsCorr<false, TIMED>(I, tm, substeps, Y, T, red, slots);
+    __syncthreads();
+  }
+}
+
 // One large cloth on a cooperative grid of CTAs (more SMs than a cluster holds): the cluster code
 // path with grid barriers; the instance's FP64 solve workspace (unused by the correction kernels)
 // holds the per-CTA slots of the team maxima.
@@ -278,6 +308,43 @@ int launchSubstepCorr(const InstanceDev* d, int count, int substeps, int smemByt
   if (timed) substepCorrKernel<true><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   else substepCorrKernel<false><<<count, kBlockThreads, smemBytes, st>>>(d, substeps, smemBytes);
   return static_cast<int>(cudaGetLastError());
+}
+
+namespace {
+template <int WT>
+int launchWork(const InstanceDev* d, int count, int* counter, int substeps, int smemBytes, cudaStream_t st,
+               bool timed) {
+  static const bool attrSet = [] {
+    cudaFuncSetAttribute(substepCorrWorkKernel<WT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(substepCorrWorkKernel<WT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return true;
+  }();
+  (void)attrSet;
+  int perSm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, substepCorrWorkKernel<WT, false>, WT, smemBytes) !=
+          cudaSuccess ||
+      perSm <= 0) {
+    cudaGetLastError();
+    return static_cast<int>(cudaErrorInvalidConfiguration);
+  }
+  const int grid = std::max(1, std::min(count, perSm * sms));  // resident CTAs only: the rest would idle
+  if (timed) substepCorrWorkKernel<WT, true><<<grid, WT, smemBytes, st>>>(d, count, counter, substeps, smemBytes);
+  else substepCorrWorkKernel<WT, false><<<grid, WT, smemBytes, st>>>(d, count, counter, substeps, smemBytes);
+  return static_cast<int>(cudaGetLastError());
+}
+}  // namespace
+
+int launchSubstepCorrWork(const InstanceDev* d, int count, int* counter, int threads, int substeps, int smemBytes,
+                          void* stream, bool timed) {
+  if (count <= 0 || substeps <= 0) return 0;
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), st);  // the table starts at its first cloth
+  if (e != cudaSuccess) return static_cast<int>(e);
+  if (threads == 512) return launchWork<512>(d, count, counter, substeps, smemBytes, st, timed);
+  if (threads == 1024) return launchWork<1024>(d, count, counter, substeps, smemBytes, st, timed);
+  return static_cast<int>(cudaErrorInvalidValue);
 }
 
 int corrClusterSupported(int cs) {

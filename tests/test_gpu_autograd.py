@@ -40,22 +40,25 @@ def _params(scene, seed=0):
 
 def test_torch_gradcheck_on_the_rollout_loss(pdg):
     """torch.autograd.gradcheck (fast mode: central differences along random directions against the
-    backward pass) on the loss normalised by its value at the start, with the parameters in scaled
-    units — stiffness relative to itself, velocities in m/s, forces in units of the vertex weight —
-    so that the step eps = 1e-6 moves every parameter by a comparable amount."""
+    backward pass) on the loss normalised by its value at the start. The checked variables are
+    displacements in scaled units, 100 × (stiffness relative to itself, velocity in m/s, force in
+    vertex weights), so that the step eps = 1e-6 moves each parameter by ~1e-4 of its scale: a
+    smaller step would only measure the rounding of the loss (every stiffness step refactorizes L,
+    and the loss is a small difference of positions), a larger one the curvature."""
     scene, prob, _ = _problem(pdg)
     kappa, v0, force = _params(scene)
-    k0 = kappa.detach().clone()
+    k0, v00, f0 = kappa.detach().clone(), v0.detach().clone(), force.detach().clone()
     weight = torch.tensor(np.asarray(scene.masses, np.float64)[:, None] * 9.81)
-    loss0 = rollout_loss(k0, v0.detach(), force.detach(), prob).item()
+    loss0 = rollout_loss(k0, v00, f0, prob).item()
     assert loss0 > 0.0
     sk = torch.zeros_like(k0, requires_grad=True)
-    sf = (force.detach() / weight).clone().requires_grad_(True)
+    sv = torch.zeros_like(v00, requires_grad=True)
+    sf = torch.zeros_like(f0, requires_grad=True)
 
-    def f(sk_, v_, sf_):
-        return rollout_loss(k0 * (1.0 + sk_), v_, weight * sf_, prob) / loss0
+    def f(sk_, sv_, sf_):
+        return rollout_loss(k0 * (1.0 + 100.0 * sk_), v00 + 100.0 * sv_, f0 + weight * (100.0 * sf_), prob) / loss0
 
-    ok = torch.autograd.gradcheck(f, (sk, v0, sf), eps=1e-6, atol=1e-8, rtol=1e-5, fast_mode=True)
+    ok = torch.autograd.gradcheck(f, (sk, sv, sf), eps=1e-6, atol=1e-8, rtol=1e-5, fast_mode=True)
     assert ok and prob.evaluations > 3
 
 

@@ -218,3 +218,32 @@ def test_batch_with_large_cloths_on_clusters(pdg):
         orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
         orc.step(20)
         assert max_rel(sim.state(i)[0], orc.state()[0]) < TOL_POS, i
+
+
+@pytest.mark.parametrize("threads", [512, 1024])
+def test_batch_as_a_work_table(pdg, threads):
+    """The MIXED batch as a work table (plan work_threads 512 / 1024): resident CTAs take the cloths
+    largest first from a counter. Every cloth matches the oracle; repeated one-substep launches (the
+    counter restarts each launch) give the bits of one multi-substep launch; a second handle with the
+    same plan gives the same bits whichever CTA took which cloth."""
+    sides = [(92, 92), (20, 24), (96, 90), (16, 40), (30, 30), (64, 70), (18, 18)]
+    scenes, cfgs = [], []
+    for nx, ny in sides:
+        cfg = with_mode(W._base(grid_nx=nx, grid_ny=ny, grid_spacing=1.0 / (max(nx, ny) - 1), max_iterations=10,
+                                shear_stiffness=900.0, bend_stiffness=20.0), "mixed")
+        scenes.append(pdg.make_grid(cfg))
+        cfgs.append(cfg)
+    sim = pdg.Simulator(scenes, cfgs)
+    sim.set_plan({"work_threads": threads})
+    assert sim.plan()["work_threads"] == threads
+    assert sim.info(0)["solve_kind"] == pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
+    for _ in range(12):
+        sim.step(1)
+    other = pdg.Simulator(scenes, cfgs)
+    other.set_plan({"work_threads": threads})
+    other.step(12)
+    for i, (s, c) in enumerate(zip(scenes, cfgs)):
+        assert np.array_equal(sim.state(i)[0].view(np.uint64), other.state(i)[0].view(np.uint64)), i
+        orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
+        orc.step(12)
+        assert max_rel(sim.state(i)[0], orc.state()[0]) < TOL_POS, i
