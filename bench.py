@@ -78,6 +78,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="mixed", choices=list(PRECISIONS))
     p.add_argument("--batch-count", type=int, default=512)
+    # CTAs per cloth for the timed handle (pd_scene_config.cluster_ctas; 0 = the planner's): e.g. 16
+    # keeps the FP64 supernodal cluster kernel on a small cloth instead of the FP64 team kernel
+    p.add_argument("--cluster-ctas", type=int, default=0)
     p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-pos-err", action="store_true")
@@ -121,7 +124,7 @@ def replica_rate(units_per_rank, seconds, world, device=None):
     return world * units_per_rank / t_max, t_max
 
 
-def workload(name, batch_count, precision="mixed"):
+def workload(name, batch_count, precision="mixed", cluster_ctas=0):
     import copy
     from pd_gb300 import workloads as W
     if name == "batch":
@@ -132,6 +135,7 @@ def workload(name, batch_count, precision="mixed"):
     cfgs = [copy.copy(c) for c in cfgs]
     for c in cfgs:
         c.precision = PRECISIONS[precision][0]
+        c.cluster_ctas = cluster_ctas
     return scenes, cfgs, sub
 
 
@@ -640,7 +644,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     import pd_gb300 as P
 
-    scenes, cfgs, sub = workload(args.workload, args.batch_count, args.precision)
+    scenes, cfgs, sub = workload(args.workload, args.batch_count, args.precision, args.cluster_ctas)
     total_count = len(scenes)
     described = describe_workload(args.workload, scenes, cfgs, sub)  # the whole workload, every rank's part
     parts = None

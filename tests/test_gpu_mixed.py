@@ -223,9 +223,9 @@ def test_batch_with_large_cloths_on_clusters(pdg):
 @pytest.mark.parametrize("threads", [512, 1024])
 def test_batch_as_a_work_table(pdg, threads):
     """The MIXED batch as a work table (plan work_threads 512 / 1024): resident CTAs take the cloths
-    largest first from a counter. Every cloth matches the oracle; repeated one-substep launches (the
-    counter restarts each launch) give the bits of one multi-substep launch; a second handle with the
-    same plan gives the same bits whichever CTA took which cloth."""
+    largest first from a counter, which restarts every launch. Every cloth matches the oracle after
+    twelve one-substep launches, and a second handle stepped the same way gives the same bits,
+    whichever CTA took which cloth."""
     sides = [(92, 92), (20, 24), (96, 90), (16, 40), (30, 30), (64, 70), (18, 18)]
     scenes, cfgs = [], []
     for nx, ny in sides:
@@ -241,7 +241,8 @@ def test_batch_as_a_work_table(pdg, threads):
         sim.step(1)
     other = pdg.Simulator(scenes, cfgs)
     other.set_plan({"work_threads": threads})
-    other.step(12)
+    for _ in range(12):
+        other.step(1)
     for i, (s, c) in enumerate(zip(scenes, cfgs)):
         assert np.array_equal(sim.state(i)[0].view(np.uint64), other.state(i)[0].view(np.uint64)), i
         orc = oracle_twin(s, c, perm=sim.factor(i)["perm"])
