@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float red[kWarps];
   __shared__ float gate;
+  __shared__ int gateHit;  // the gate's decision, taken once by thread 0 and read by every thread
   __shared__ int failed;
   const int rank = static_cast<int>(blockIdx.x) % team;
   const InstanceDev& I = insts[blockIdx.x / team];
@@ -348,6 +349,9 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
+        // the residual gate's decision, in FP64 as the reference takes it, by one thread: on this part
+        // an FP64 instruction costs every warp that issues it ~80 cycles of its FP64 pipe
+        if (lane == 0) gateHit = (k >= 1 && static_cast<double>(gate) <= I.resThreshold) ? 1 : 0;
       } else {
         ok = pollWords<10>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
           const int v = j / 3;
@@ -357,14 +361,18 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
-      const double gateA = gate;
-      if (k == 0) scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
+      if (k == 0) {
+        const double gateA = gate;
+        scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
+      }
       bool stop = k == I.maxIter;
       if (I.useResidual && k >= 1) {
-        lastRes = gateA;
         used = k;
-        if (I.resTrace && rank == 0 && threadIdx.x == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gateA;
-        conv = gateA <= I.resThreshold;
+        if (threadIdx.x == 0) {  // the only thread that reports them
+          lastRes = gate;
+          if (I.resTrace && rank == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gate;
+        }
+        conv = gateHit != 0;
         stop = stop || conv;
       }
       if (stop) {
@@ -425,6 +433,11 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
           }
           __syncwarp();
           ok = pollPartials(ptagB, team, tagB, &gate);
+          if (lane == 0) {  // the displacement gate's decision, once
+            const double diff = gate;
+            const double rel = (scale > 0.0) ? diff / scale : diff;
+            gateHit = ((I.absTol > 0.0) && (diff <= I.absTol)) || ((I.relTol > 0.0) && (rel <= I.relTol)) ? 1 : 0;
+          }
         } else {
           ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
             const int v = j / 6, c = j - 6 * v;  // c < 3: hi, else lo
@@ -474,12 +487,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         __syncthreads();
       }
       if (!I.useResidual) {
-        const double diff = gate;
-        const double rel = (scale > 0.0) ? diff / scale : diff;
-        const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
-        const bool relHit = (I.relTol > 0.0) && (rel <= I.relTol);
         used = k + 1;
-        conv = absHit || relHit;
+        conv = gateHit != 0;
         if (conv) break;
       }
     }

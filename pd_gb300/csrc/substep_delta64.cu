@@ -303,6 +303,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[kWarps];
   __shared__ double gate;
+  __shared__ int gateHit;  // the gate's decision, taken once by thread 0 and read by every thread
   __shared__ int failed;
   const int rank = static_cast<int>(blockIdx.x) % team;
   const InstanceDev& I = insts[blockIdx.x / team];
@@ -481,6 +482,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
+        if (lane == 0) gateHit = (k >= 1 && gate <= I.resThreshold) ? 1 : 0;  // one FP64 compare, not one a warp
       } else {
         ok = pollValues<5>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32,
                            [&](int j, unsigned wh, unsigned wl) {  // r as its FP32 pair
@@ -492,14 +494,15 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
       if (!ok) failed = 1;
       __syncthreads();
       if (failed) break;
-      const double gateA = gate;
-      if (k == 0) scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
+      if (k == 0) scale = (gate < I.gScaleHH) ? I.gScaleHH : gate;
       bool stop = k == I.maxIter;
       if (I.useResidual && k >= 1) {
-        lastRes = gateA;
         used = k;
-        if (I.resTrace && rank == 0 && threadIdx.x == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gateA;
-        conv = gateA <= I.resThreshold;
+        if (threadIdx.x == 0) {  // the only thread that reports them
+          lastRes = gate;
+          if (I.resTrace && rank == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gate;
+        }
+        conv = gateHit != 0;
         stop = stop || conv;
       }
       if (stop) {
@@ -565,6 +568,11 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
           }
           __syncwarp();
           ok = pollPartials(ptagB, team, tagB, &gate);
+          if (lane == 0) {  // the displacement gate's decision, once
+            const double diff = gate;
+            const double rel = (scale > 0.0) ? diff / scale : diff;
+            gateHit = ((I.absTol > 0.0) && (diff <= I.absTol)) || ((I.relTol > 0.0) && (rel <= I.relTol)) ? 1 : 0;
+          }
         } else {
           ok = pollValues<3>(I.xtag, 3 * wlo, 3 * whi, tagB, threadIdx.x - 32, blockDim.x - 32, sinkX);
         }
@@ -576,12 +584,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
       if (failed) break;
       clk.lap(I, rank == 0 && threadIdx.x == 0, kStageUnpack);  // the update and exchange B (the window's positions)
       if (!I.useResidual) {
-        const double diff = gate;
-        const double rel = (scale > 0.0) ? diff / scale : diff;
-        const bool absHit = (I.absTol > 0.0) && (diff <= I.absTol);
-        const bool relHit = (I.relTol > 0.0) && (rel <= I.relTol);
         used = k + 1;
-        conv = absHit || relHit;
+        conv = gateHit != 0;
         if (conv) break;
       }
     }
