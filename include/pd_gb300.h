@@ -224,12 +224,13 @@ typedef struct pd_sim_info {
                                     by a team of co-resident CTAs per cloth */
 #define PD_SOLVE_SUPERNODAL32_CORRECTION 5 /* MIXED: FP32 supernodes applied to the correction
                                               b − Ã·x, one CTA per cloth */
-#define PD_SOLVE_DENSE64_TEAM 6  /* FP64 (small cloths, no over-relaxation): the explicit inverse applied
-                                    to the FP64 correction b − Ã·x in double-float arithmetic (FP32
-                                    pairs, error-free products and sums) by a team of co-resident CTAs
-                                    per cloth; FP64-accurate positions, residual and gate. A requested
-                                    cluster of 1-16 CTAs (cluster_ctas, pd_plan) or dense_max_vertices
-                                    < 0 keeps PD_SOLVE_SUPERNODAL */
+#define PD_SOLVE_DENSE64_TEAM 6  /* FP64 and FP32_PROJECTION (small cloths, no over-relaxation): the
+                                    explicit inverse applied to the FP64 correction b − Ã·x in
+                                    double-float arithmetic (FP32 pairs, error-free products and sums)
+                                    by a team of co-resident CTAs per cloth; FP64-accurate positions,
+                                    residual and gate (FP32_PROJECTION: the projection d_e in FP32). A
+                                    requested cluster of 1-16 CTAs (cluster_ctas, pd_plan) or
+                                    dense_max_vertices < 0 keeps PD_SOLVE_SUPERNODAL */
 
 typedef struct pd_sim_stats {    /* SimContext counters (core/sim/Scene.h:161-169) */
   int32_t iterations_used;       /* of the last substep */

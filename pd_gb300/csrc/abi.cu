@@ -712,7 +712,7 @@ struct pd_sim {
     delta64 = false;
     corr = false;
     if (p == PD_PRECISION_FP64_EXACT) return;
-    if (p == PD_PRECISION_FP64 && planDelta64()) return;
+    if (supernodalFp64(p) && planDelta64()) return;  // FP64, and FP32 projection with the FP64 solve
     for (auto& I : inst) {
       I.corrTeam = 1;
       I.corrThreads = pdg::kBlockThreads;

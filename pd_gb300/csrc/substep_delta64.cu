@@ -25,6 +25,8 @@
 // bits), each checked for the current epoch. r and the A partials alternate between two buffers.
 // Every poll gives up after a bounded number of rounds, sets the instance's error flag and ends the
 // CTA. Chebyshev-weighted iterates are not taken here (the planner keeps the supernodal kernel then).
+// The same kernel serves PD_PRECISION_FP32_PROJECTION on small cloths: the projection d_e in FP32,
+// the correction, the solve and the residual as above.
 #include <cstdint>
 
 #include <algorithm>
@@ -254,15 +256,32 @@ __device__ __forceinline__ double restOverLength(double dot, double rest) {
 // The terms of one edge incidence of own vertex v (other vertex o, FP64): κ·((x_v − x_o) − d_e) into
 // t[0..2] and, when o is pinned, what the matrix adds by seeing o at q, κ·((x_v − q_o) − (x_v − x_o)),
 // into t[3..5] (zeros otherwise). d_e = ℓ·rel/‖rel‖, zero when ‖rel‖ ≤ 1e-12 (DistanceTerm.cpp:94-102).
+// With I.proj32 (PD_PRECISION_FP32_PROJECTION) d_e itself is FP32, from the FP64 difference, as in
+// the supernodal kernels' projectEdge; everything else stays FP64.
 __device__ __forceinline__ void edgeIncidence(const InstanceDev& I, const double* xv, const double* xo, int oo,
                                               double rest, double kap, double* t) {
   const double rx = xv[0] - xo[0], ry = xv[1] - xo[1], rz = xv[2] - xo[2];
-  const double dot = fma(rx, rx, fma(ry, ry, rz * rz));
-  double sc = 0.0;
-  if (!(dot <= 1e-24)) sc = restOverLength(dot, rest);
-  t[0] = kap * (rx - rx * sc);
-  t[1] = kap * (ry - ry * sc);
-  t[2] = kap * (rz - rz * sc);
+  if (I.proj32) {
+    const float fx = static_cast<float>(rx), fy = static_cast<float>(ry), fz = static_cast<float>(rz);
+    const float len = sqrtf(fx * fx + fy * fy + fz * fz);
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    if (!(len <= 1e-12f)) {
+      const float s = static_cast<float>(rest) / len;
+      dx = fx * s;
+      dy = fy * s;
+      dz = fz * s;
+    }
+    t[0] = kap * (rx - static_cast<double>(dx));
+    t[1] = kap * (ry - static_cast<double>(dy));
+    t[2] = kap * (rz - static_cast<double>(dz));
+  } else {
+    const double dot = fma(rx, rx, fma(ry, ry, rz * rz));
+    double sc = 0.0;
+    if (!(dot <= 1e-24)) sc = restOverLength(dot, rest);
+    t[0] = kap * (rx - rx * sc);
+    t[1] = kap * (ry - ry * sc);
+    t[2] = kap * (rz - rz * sc);
+  }
   if (oo < 0) {
     const int o = oo & 0x7fffffff;
     t[3] = kap * ((xv[0] - __ldg(I.q + 3 * o)) - rx);

@@ -34,8 +34,8 @@ def with_mode(cfg, mode, ctas=0, dense=0):
 
 def expected_kind(pdg, mode, ctas, dense):
     m = MODES[mode]
-    if m == pdg.PD_PRECISION_FP32_PROJECTION:
-        return pdg.PD_SOLVE_SUPERNODAL
+    if m == pdg.PD_PRECISION_FP32_PROJECTION:  # the FP64 team kernel unless a cluster is asked for
+        return pdg.PD_SOLVE_DENSE64_TEAM if (ctas == 0 and dense >= 0) else pdg.PD_SOLVE_SUPERNODAL
     if m == pdg.PD_PRECISION_MIXED:  # a team on the explicit inverse, else one CTA in correction form
         return pdg.PD_SOLVE_DENSE32_TEAM if (ctas != 1 and dense >= 0) else pdg.PD_SOLVE_SUPERNODAL32_CORRECTION
     return pdg.PD_SOLVE_SUPERNODAL32 if (ctas == 1 or dense < 0) else pdg.PD_SOLVE_DENSE32
@@ -46,8 +46,8 @@ def expected_kind(pdg, mode, ctas, dense):
 def test_plain_cloth_600_substeps(pdg, mode, strategy):
     scenes, cfg, substeps = W.cloth40_plain()
     ctas, dense = STRATEGIES[strategy]
-    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION and strategy in ("cluster-dense", "auto"):
-        pytest.skip("the FP64 solve has no dense variant")
+    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION and strategy == "cluster-dense":
+        pytest.skip("a 16-CTA request keeps the FP64 supernodal cluster: the same as cluster-supernodal")
     sim = pdg.Simulator(scenes[0], with_mode(cfg, mode, ctas, dense))
     assert sim.info()["solve_kind"] == expected_kind(pdg, mode, ctas, dense)
     orc = oracle_twin(scenes[0], cfg, perm=sim.factor()["perm"])
@@ -59,11 +59,13 @@ def test_plain_cloth_600_substeps(pdg, mode, strategy):
     assert np.array_equal(sim.state()[0][pins], scenes[0].positions[pins])
 
 
-@pytest.mark.parametrize("mode", ["mixed", "fp32-solve"])
+@pytest.mark.parametrize("mode", ["mixed", "fp32-solve", "fp32-projection"])
 @pytest.mark.parametrize("strategy", list(STRATEGIES))
 def test_full_cloth_600_substeps(pdg, mode, strategy):
     scenes, cfg, substeps = W.cloth40_full()
     ctas, dense = STRATEGIES[strategy]
+    if MODES[mode] == pdg.PD_PRECISION_FP32_PROJECTION and strategy == "cluster-dense":
+        pytest.skip("a 16-CTA request keeps the FP64 supernodal cluster: the same as cluster-supernodal")
     sim = pdg.Simulator(scenes[0], with_mode(cfg, mode, ctas, dense))
     assert sim.info()["solve_kind"] == expected_kind(pdg, mode, ctas, dense)
     orc = oracle_twin(scenes[0], cfg, perm=sim.factor()["perm"])
