@@ -831,17 +831,16 @@ def _cpu_gradient_worker(job):
     """One spawned process: builds differentiable problem `i` with the oracle alone (targets from an
     oracle run at the hidden κ*), waits for the others, then times one serial FP64 adjoint."""
     i, barrier = job
-    from tests.helpers import oracle_twin  # checker only
-    from pd_gb300 import workloads as W
-    scene, cfg, S, _ = W.differentiable()
-    twin = oracle_twin(scene, cfg, threads=1)
-    twin.set_edge_stiffness(W.differentiable(seed=i + 1)[3])
+    from oracle import oracle as O, workloads as OW  # checker / CPU baseline only
+    mesh, cfg, S, _ = OW.differentiable(threads=1)
+    twin = O.OracleSim(mesh, cfg)
+    twin.set_edge_stiffness(OW.differentiable(seed=i + 1)[3])
     twin.step(S)
     target = twin.state()[0]
-    orc = oracle_twin(scene, cfg, threads=1)
+    orc = O.OracleSim(mesh, cfg)
     barrier.wait()
     t0 = time.perf_counter()
-    orc.gradient(S, target, np.zeros((scene.n, 3)))
+    orc.gradient(S, target, np.zeros((mesh.n, 3)))
     return time.perf_counter() - t0
 
 
@@ -990,8 +989,8 @@ def run_reference_gradients(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from pd_gb300 import workloads as W
-    scene, _, S, _ = W.differentiable()
+    from oracle import workloads as OW  # the reference arm loads nothing of the product
+    scene, _, S, _ = OW.differentiable()
     steps = max(1, min(args.steps, 3))
     runs = [cpu_gradients() for _ in range(steps)]
     value = statistics.median(r["value"] for r in runs)

@@ -20,9 +20,10 @@
 // its incidences and its rows of Ã⁻¹ in shared memory. Per iteration: the correction pass of own
 // vertices → exchange A (the whole r and the maximum of the residuals: a full barrier) → own rows of
 // Ã⁻¹·r → update of own positions → exchange B (the positions of the CTA's window: its vertices, edge
-// neighbours and bend partners). An exchange word is (epoch << 32 | 32 bits of data), written and
-// polled with relaxed gpu-scope accesses; an FP64 value travels as two words (its low and high 32
-// bits), each checked for the current epoch. r and the A partials alternate between two buffers.
+// neighbours and bend partners). An exchange word carries the epoch it was written in and its data,
+// written and polled with relaxed gpu-scope accesses: a position or a partial maximum travels as two
+// words (epoch << 32 | low or high 32 bits of the FP64), an r value as one packed word (packR). r and
+// the A partials alternate between two buffers.
 // Every poll gives up after a bounded number of rounds, sets the instance's error flag and ends the
 // CTA. Chebyshev-weighted iterates are not taken here (the planner keeps the supernodal kernel then).
 // The same kernel serves PD_PRECISION_FP32_PROJECTION on small cloths: the projection d_e in FP32,
@@ -108,6 +109,51 @@ __device__ __forceinline__ bool pollValues(const unsigned long long* src, int b,
 // are taken with integer operations: on this part an FP64 warp instruction occupies its sub-core's
 // FP64 pipe for ~80 cycles whatever its active lanes, and these reductions would otherwise be a
 // large share of an iteration. A NaN counts as 0 (it is skipped, as the reference's `>` skips it).
+// r travels as one word: an 8-bit epoch tag, the FP32 hi part and the top 24 bits of the FP32 lo
+// part rounded to nearest (sign, exponent, 15 mantissa bits): hi + lo keeps r to ~2⁻³⁹ relative, and
+// Δ = Ã⁻¹·r, a correction, to far below the FP64 rounding of the positions. A word is rewritten every
+// fourth epoch, so its tag is never more than 4 behind the current one and 8 bits tell them apart.
+__device__ __forceinline__ unsigned long long packR(unsigned tag, float hi, float lo) {
+  const unsigned lo24 = (__float_as_uint(lo) + 0x80u) >> 8;
+  return (static_cast<unsigned long long>(tag & 0xffu) << 56) |
+         (static_cast<unsigned long long>(__float_as_uint(hi)) << 24) | lo24;
+}
+
+// Polls the packed words [b, e) of src until each carries the current 8-bit tag and hands
+// sink(j, hi, lo) the pair; B words in flight per thread. False after kSpinLimit stale rounds.
+template <int B, class Sink>
+__device__ __forceinline__ bool pollPacked(const unsigned long long* src, int b, int e, unsigned tag, int tid,
+                                           int nth, Sink&& sink) {
+  const unsigned t8 = tag & 0xffu;
+  for (int j0 = b + tid; j0 < e; j0 += B * nth) {
+    unsigned pending = 0;
+#pragma unroll
+    for (int u = 0; u < B; ++u)
+      if (j0 + u * nth < e) pending |= 1u << u;
+    long long spins = 0;
+    unsigned nap = 32;
+    while (pending) {
+      unsigned long long w[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) w[u] = ((pending >> u) & 1u) ? loadRelaxed(src + j0 + u * nth) : 0ull;
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        if (((pending >> u) & 1u) && static_cast<unsigned>(w[u] >> 56) == t8) {
+          sink(j0 + u * nth, __uint_as_float(static_cast<unsigned>(w[u] >> 24)),
+               __uint_as_float(static_cast<unsigned>(w[u] & 0xffffffull) << 8));
+          pending &= ~(1u << u);
+        }
+      }
+      if (pending) {
+        if (++spins > kSpinLimit) return false;
+        __nanosleep(nap);
+        nap = min(2 * nap, 256u);
+      }
+    }
+  }
+  return true;
+}
+
 __device__ __forceinline__ long long maxKey(double v) {
   const long long b = __double_as_longlong(v);
   return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? 0ll : b;
@@ -435,7 +481,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
     for (int k = 0;; ++k) {
       const unsigned tagA = ++epoch;  // odd: epochs are consumed in (A, B) pairs
       const unsigned buf = (tagA >> 1) & 1u;
-      unsigned long long* rtag = I.rtag + static_cast<size_t>(buf) * 6 * n;
+      unsigned long long* rtag = I.rtag + static_cast<size_t>(buf) * 3 * n;
       unsigned long long* ptagA = I.ptag + buf * kPartStride * team;
       // correction r and residual of x^k for own vertices (FP64; Integrator.cpp:230-263 for the
       // residual): one lane per incidence computes its terms, then three lanes per vertex sum them in
@@ -473,10 +519,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
         tres[t] = tv;
         const float hi = __double2float_rn(r);
         const float lo = __double2float_rn(r - static_cast<double>(hi));
-        unsigned long long* w = rtag + 2 * (3 * static_cast<size_t>(v) + c);
-        const unsigned long long tg = static_cast<unsigned long long>(tagA) << 32;
-        storeRelaxed(w, tg | __float_as_uint(hi));
-        storeRelaxed(w + 1, tg | __float_as_uint(lo));
+        storeRelaxed(rtag + 3 * static_cast<size_t>(v) + c, packR(tagA, hi, lo));
       }
       __syncthreads();
       double resLocal = 0.0;
@@ -503,12 +546,12 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDelta64Kernel(const I
         ok = pollPartials(ptagA, team, tagA, &gate);
         if (lane == 0) gateHit = (k >= 1 && gate <= I.resThreshold) ? 1 : 0;  // one FP64 compare, not one a warp
       } else {
-        ok = pollValues<5>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32,
-                           [&](int j, unsigned wh, unsigned wl) {  // r as its FP32 pair
-                             const int v = j / 3, c = j - 3 * v;
-                             Rh[c * ld + v] = __uint_as_float(wh);
-                             Rl[c * ld + v] = __uint_as_float(wl);
-                           });
+        ok = pollPacked<10>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32,
+                            [&](int j, float hi, float lo) {  // r as its FP32 pair
+                              const int v = j / 3, c = j - 3 * v;
+                              Rh[c * ld + v] = hi;
+                              Rl[c * ld + v] = lo;
+                            });
       }
       if (!ok) failed = 1;
       __syncthreads();
