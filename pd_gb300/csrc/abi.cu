@@ -243,9 +243,10 @@ int deltaSmem(const Instance& I, int team, int* resRows) {
   teamCaps(I, team, &eCap, &bCap);
   const int wCap = teamWindowCap(I, team);
   // positions, correction, incidences, vertex constants, FP64 state, Δ, incidence offsets
-  // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 24·chunk partial sums of Δ over
-  // up to two column segments), and the window's previous positions (over-relaxed iterations)
-  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + 120L * chunk + 8L * (chunk + 1) + 32L * wCap;
+  // (16·chunk vertex constants, 32·chunk x̂, 48·chunk x_n and v, 12·chunk partial sums of Δ per
+  // product warp), and the window's previous positions (over-relaxed iterations)
+  const long fixed = 32L * n + 12L * ld + 16L * (eCap + bCap) + (96L + 12L * pdg::kDeltaProductWarps) * chunk +
+                     8L * (chunk + 1) + 32L * wCap;
   long rows = fixed < kDeltaSmem ? (kDeltaSmem - fixed) / (4L * ld) : 0;
   if (rows >= chunk) {
     rows = chunk;

@@ -248,6 +248,9 @@ int launchSubstepCorrWork(const InstanceDev* dInstances, int count, int* counter
                           int smemBytes, void* stream, bool timed = false);
 int corrGridCapacity();
 constexpr int kDeltaThreads = 512;
+// warps of the MIXED team kernel that apply the CTA's rows of Ã⁻¹, each leaving a partial sum per row
+// and component in shared memory
+constexpr int kDeltaProductWarps = 8;
 
 // FP64 team kernel (substep_delta64.cu) on `team` CTAs of kDeltaThreads threads per cloth, the
 // correction form with Ã⁻¹·r in double-float arithmetic; delta64ResidentCtas as deltaResidentCtas.

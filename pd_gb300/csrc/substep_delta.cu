@@ -27,7 +27,10 @@
 // epoch, so an exchange costs about one L2 round trip after the last writer and needs no fence
 // (a fence would also drop the L1 lines the CTA reads through). Per-CTA partial maxima (residual,
 // displacement, scale) travel the same way, one per L2 line; one warp polls them while the
-// others poll the data words, backing off between rounds so that waiting CTAs do not flood L2.
+// others poll the data words. Polling does not back off: a store is visible to another SM about
+// 250 ns later on the same die and 370 ns on the other, and a sleep between rounds only adds to
+// that; each round waits for its own loads, so a waiting CTA keeps at most a few loads in flight
+// per thread.
 // Exchange A is a full barrier of the team; with the residual gate exchange B only waits for
 // the CTAs whose positions a CTA reads, so r and the A partials alternate between two buffers.
 // Every word is rewritten only after a later full barrier, which no CTA passes before every CTA
@@ -44,11 +47,10 @@ namespace pdg {
 namespace {
 
 constexpr int kWarps = kDeltaThreads / 32;
-constexpr int kGroup = 16;                  // lanes per vertex in the correction pass
 constexpr long long kSpinLimit = 1ll << 22; // poll rounds before an exchange gives up
 constexpr int kMaxTeam = 256;               // partials one polling warp covers (kMaxTeam / 32 a lane)
-constexpr int kSegments = 2;                // most column segments a row group of Ã⁻¹ is split into
-constexpr int kGroupRows = 2;               // rows of Ã⁻¹ one warp applies together
+constexpr int kGroup = 16;                  // lanes per vertex in the correction pass
+constexpr int kRowBlock = 11;               // rows of Ã⁻¹ one warp applies together (33 sums, one transpose)
 constexpr int kPartStride = 16;             // words between two CTAs' partials: one L2 line each
 
 __device__ __forceinline__ unsigned long long loadRelaxed(const unsigned long long* p) {
@@ -77,7 +79,6 @@ __device__ __forceinline__ bool pollWords(const unsigned long long* src, int b, 
     for (int u = 0; u < B; ++u)
       if (j0 + u * nth < e) pending |= 1u << u;
     long long spins = 0;
-    unsigned nap = 32;  // back off while words are stale, so waiting CTAs do not flood L2
     while (pending) {
       unsigned long long w[B];
 #pragma unroll
@@ -89,11 +90,7 @@ __device__ __forceinline__ bool pollWords(const unsigned long long* src, int b, 
           pending &= ~(1u << u);
         }
       }
-      if (pending) {
-        if (++spins > kSpinLimit) return false;
-        __nanosleep(nap);
-        nap = min(2 * nap, 256u);
-      }
+      if (pending && ++spins > kSpinLimit) return false;
     }
   }
   return true;
@@ -117,7 +114,6 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
     if (first + step * (lane + 32 * i) < team) pending |= 1u << i;
   float mx = 0.f;
   long long spins = 0;
-  unsigned nap = 32;
   bool good = true;
   while (true) {
     unsigned long long w[kMaxTeam / 32];
@@ -136,8 +132,6 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
       good = false;
       break;
     }
-    __nanosleep(nap);
-    nap = min(2 * nap, 256u);
   }
   mx = warpMaxF(mx);
   if (lane == 0) *out = mx;
@@ -157,44 +151,81 @@ __device__ __forceinline__ double warpMaxD(double v) {
   return v;
 }
 
-// Up to NR rows of Ã⁻¹ (starting at A0, nr of them) times the three components of R over the
-// float4 columns [jb, je), one warp; each R load serves NR rows. A rows from shared or global
-// memory. Sums land in dl[3·(li + r) + c].
-template <int NR, bool SMEM>
-__device__ __forceinline__ void rowGroup(const float* A0, int nr, const float* Rs, int ld, int li, int jb, int je,
-                                         float* dl) {
+// The displacement gate (Integrator.cpp:676-699) on the FP32 maximum g of the iteration's
+// displacements: diff = (double)g passes when diff ≤ absTol or diff / scale ≤ relTol (diff itself
+// when scale ≤ 0), each test only when its tolerance is positive. Both are monotone in g, so each
+// holds exactly when g is at most the largest float that passes it; those thresholds are found once
+// per substep (a failing test gets −∞).
+__device__ __noinline__ void displacementThresholds(double absTol, double relTol, double scale, float* absF,
+                                                    float* relF) {
+  *absF = (absTol > 0.0) ? __double2float_rd(absTol) : -INFINITY;
+  if (!(relTol > 0.0)) {
+    *relF = -INFINITY;
+    return;
+  }
+  if (!(scale > 0.0)) {
+    *relF = __double2float_rd(relTol);
+    return;
+  }
+  auto passes = [&](float g) { return static_cast<double>(g) / scale <= relTol; };
+  float t = __double2float_rd(relTol * scale);
+  for (int i = 0; i < 64 && !passes(t) && t > -INFINITY; ++i) t = nextafterf(t, -INFINITY);
+  for (int i = 0; i < 64 && t < INFINITY && passes(nextafterf(t, INFINITY)); ++i) t = nextafterf(t, INFINITY);
+  *relF = t;
+}
+
+// One step of a transposing warp reduction: lanes with bit O set keep the upper half of s[0, 2·O),
+// the others the lower half, each adding the half its partner sends.
+template <int O>
+__device__ __forceinline__ void transposeStep(float* s, int lane) {
+  const bool up = (lane & O) != 0;
+#pragma unroll
+  for (int i = 0; i < O; ++i) {
+    const float send = up ? s[i] : s[i + O];
+    const float keep = up ? s[i + O] : s[i];
+    s[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+  }
+}
+
+// Rows [0, nr) (nr ≤ kRowBlock) of Ã⁻¹ starting at A0 (shared or global memory) times the three
+// components of R, by warp `w` of `nw`: lane l takes the float4 columns w·32 + l, w·32 + l + 32·nw, ...
+// so that R and the rows are read once by the nw warps together; the 3·nr sums are then reduced
+// over the warp in 31 + 5 shuffles (a transpose of the first 32 and a butterfly of the last) and
+// written to out[3·r + c], the warp's share of the row products.
+template <bool SMEM, bool FULL>
+__device__ __forceinline__ void rowBlock(const float* A0, int nrArg, const float* Rs, int ld, int w, int nw, float* out) {
+  const int nr = FULL ? kRowBlock : nrArg;  // a full block has no per-row predicates
   const int lane = threadIdx.x & 31;
   const float4* a = reinterpret_cast<const float4*>(A0);
   const int ld4 = ld / 4;
   const float4* rx = reinterpret_cast<const float4*>(Rs);
   const float4* ry = reinterpret_cast<const float4*>(Rs + ld);
   const float4* rz = reinterpret_cast<const float4*>(Rs + 2 * ld);
-  float s[NR][3];
+  float s[3 * kRowBlock];
 #pragma unroll
-  for (int r = 0; r < NR; ++r) s[r][0] = s[r][1] = s[r][2] = 0.f;
-#pragma unroll 4
-  for (int j = jb + lane; j < je; j += 32) {
+  for (int i = 0; i < 3 * kRowBlock; ++i) s[i] = 0.f;
+  for (int j = 32 * w + lane; j < ld4; j += 32 * nw) {
     const float4 x = rx[j], y = ry[j], z = rz[j];
 #pragma unroll
-    for (int r = 0; r < NR; ++r) {
+    for (int r = 0; r < kRowBlock; ++r) {
       if (r < nr) {
         const float4 u = SMEM ? a[r * ld4 + j] : __ldg(a + r * ld4 + j);
-        s[r][0] = fmaf(u.x, x.x, fmaf(u.y, x.y, fmaf(u.z, x.z, fmaf(u.w, x.w, s[r][0]))));
-        s[r][1] = fmaf(u.x, y.x, fmaf(u.y, y.y, fmaf(u.z, y.z, fmaf(u.w, y.w, s[r][1]))));
-        s[r][2] = fmaf(u.x, z.x, fmaf(u.y, z.y, fmaf(u.z, z.z, fmaf(u.w, z.w, s[r][2]))));
+        s[3 * r] = fmaf(u.x, x.x, fmaf(u.y, x.y, fmaf(u.z, x.z, fmaf(u.w, x.w, s[3 * r]))));
+        s[3 * r + 1] = fmaf(u.x, y.x, fmaf(u.y, y.y, fmaf(u.z, y.z, fmaf(u.w, y.w, s[3 * r + 1]))));
+        s[3 * r + 2] = fmaf(u.x, z.x, fmaf(u.y, z.y, fmaf(u.z, z.z, fmaf(u.w, z.w, s[3 * r + 2]))));
       }
     }
   }
+  transposeStep<16>(s, lane);
+  transposeStep<8>(s, lane);
+  transposeStep<4>(s, lane);
+  transposeStep<2>(s, lane);
+  transposeStep<1>(s, lane);  // lane l now holds the warp's sum of s[l]
+  float e = s[32];
 #pragma unroll
-  for (int r = 0; r < NR; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) s[r][c] = groupSum<32>(s[r][c]);
-  if (lane == 0)
-#pragma unroll
-    for (int r = 0; r < NR; ++r)
-      if (r < nr)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) dl[3 * (li + r) + c] = s[r][c];
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if (lane < 3 * nr) out[lane] = s[0];
+  if (lane == 0 && 3 * nr > 32) out[32] = e;
 }
 
 template <bool TIMED>
@@ -204,6 +235,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   __shared__ float red[kWarps];
   __shared__ float gate;
   __shared__ int gateHit;  // the gate's decision, taken once by thread 0 and read by every thread
+  __shared__ float dispAbsF, dispRelF;  // the displacement gate's thresholds on the FP32 maximum
   __shared__ int failed;
   const int rank = static_cast<int>(blockIdx.x) % team;
   const InstanceDev& I = insts[blockIdx.x / team];
@@ -227,8 +259,8 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   float4* sXp = sXh + 2 * chunk;  // window positions before an over-relaxed update (teamWCap pairs)
   double* xn64 = reinterpret_cast<double*>(sXp + 2 * I.teamWCap);
   double* v64 = xn64 + 3 * chunk;
-  float* dl = reinterpret_cast<float*>(v64 + 3 * chunk);  // kSegments × 3·chunk
-  int* sEb = reinterpret_cast<int*>(dl + kSegments * 3 * chunk);
+  float* dl = reinterpret_cast<float*>(v64 + 3 * chunk);  // kDeltaProductWarps × 3·chunk
+  int* sEb = reinterpret_cast<int*>(dl + kDeltaProductWarps * 3 * chunk);
   int* sBb = sEb + chunk + 1;
 
   if (threadIdx.x == 0) failed = 0;
@@ -263,10 +295,17 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
   // the residual gate exchange B only waits for the CTAs whose positions a CTA reads
   unsigned long long* ptagB = I.ptag + 2 * kPartStride * team;
   const int wlo = I.window[2 * rank], whi = I.window[2 * rank + 1];
-  // GEMV work: row pairs × column segments over the warps
-  const int groups = (m + kGroupRows - 1) / kGroupRows;
-  const int segs = groups > 0 ? max(1, min(kSegments, kWarps / groups)) : 1;
-  const int q4 = ld / 4;
+  // loop invariants kept in registers (the relaxed accesses' memory clobbers would reload them)
+  const int useRes = I.useResidual, maxIter = I.maxIter, chebFrom = I.chebFrom, withhold = I.withholdRank;
+  unsigned long long* const rtagBase = I.rtag;
+  unsigned long long* const ptagBase = I.ptag;
+  unsigned long long* const xtag = I.xtag;
+  const double* const omegaP = I.omega;
+  double* const resTraceP = I.resTrace;
+  const float* const qf = reinterpret_cast<const float*>(I.qhl);
+  float* const xhf = reinterpret_cast<float*>(sXh);  // x̂ of own vertex li: hi at 8·li + c, lo at 8·li + 4 + c
+  // the residual gate in FP32: for a float g, (double)g ≤ T exactly when g ≤ T rounded down to a float
+  const float resThrF = __double2float_rd(I.resThreshold);
   __syncthreads();
 
   const StageClock<TIMED> clk(I, rank == 0 && threadIdx.x == 0);
@@ -280,7 +319,6 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       xn64[t] = p;
       float hi, lo;
       split(xh, hi, lo);
-      float* xhf = reinterpret_cast<float*>(sXh);
       xhf[8 * li + c] = hi;
       xhf[8 * li + 4 + c] = lo;
       sc = fmax(sc, fabs(xh - p));
@@ -291,21 +329,21 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
     double scale = 0.0;
     int used = 0;
     bool conv = false;
-    double lastRes = I.useResidual ? 0.0 : -1.0;
+    float lastRes = I.useResidual ? 0.f : -1.f;  // the gate's FP32 maximum (exact in FP64)
     float resSplit = 0.f;  // residual of the last over-relaxed iteration's solve (per thread)
     for (int k = 0;; ++k) {
       // an over-relaxed iteration with the residual gate (Integrator.cpp:631-663) puts x^k + Δ,
       // takes that point's residual, then adds (ω − 1)·Δ to every window vertex
-      const bool blend = k >= I.chebFrom && k < I.maxIter;
-      const bool split = blend && I.useResidual;
-      const bool splitBefore = I.useResidual && k >= 1 && k - 1 >= I.chebFrom;
-      const float om = blend ? static_cast<float>(I.omega[k]) : 1.f;
+      const bool blend = k >= chebFrom && k < maxIter;
+      const bool split = blend && useRes;
+      const bool splitBefore = useRes && k >= 1 && k - 1 >= chebFrom;
+      const float om = blend ? static_cast<float>(omegaP[k]) : 1.f;
       if (split)
         for (int t = threadIdx.x; t < 2 * (whi - wlo); t += blockDim.x) sXp[t] = Xs[2 * wlo + t];
       const unsigned tagA = ++epoch;  // odd: epochs are consumed in (A, B) pairs
       const unsigned buf = (tagA >> 1) & 1u;
-      unsigned long long* rtag = I.rtag + buf * 3 * n;
-      unsigned long long* ptagA = I.ptag + buf * kPartStride * team;
+      unsigned long long* rtag = rtagBase + buf * 3 * n;
+      unsigned long long* ptagA = ptagBase + buf * kPartStride * team;
       // correction r and residual of x^k for own vertices, kGroup lanes per vertex (FP32 only)
       float resLocal = 0.f;
       const int gl = threadIdx.x & (kGroup - 1), group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
@@ -344,14 +382,13 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         if (lane == 0) {
           float pm = 0.f;
           for (int w = 0; w < kWarps; ++w) pm = fmaxf(pm, red[w]);
-          if (!(I.withholdRank == rank && step == 0 && k == 0))
+          if (!(withhold == rank && step == 0 && k == 0))
             storeRelaxed(ptagA + kPartStride * rank, tagged(tagA, pm));
         }
         __syncwarp();
         ok = pollPartials(ptagA, team, tagA, &gate);
-        // the residual gate's decision, in FP64 as the reference takes it, by one thread: on this part
-        // an FP64 instruction costs every warp that issues it ~80 cycles of its FP64 pipe
-        if (lane == 0) gateHit = (k >= 1 && static_cast<double>(gate) <= I.resThreshold) ? 1 : 0;
+        // the residual gate's decision (the reference's FP64 comparison, taken exactly in FP32), once
+        if (lane == 0) gateHit = (k >= 1 && gate <= resThrF) ? 1 : 0;
       } else {
         ok = pollWords<10>(rtag, 0, 3 * n, tagA, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
           const int v = j / 3;
@@ -364,13 +401,14 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
       if (k == 0) {
         const double gateA = gate;
         scale = (gateA < I.gScaleHH) ? I.gScaleHH : gateA;
+        if (threadIdx.x == 0 && !useRes) displacementThresholds(I.absTol, I.relTol, scale, &dispAbsF, &dispRelF);
       }
-      bool stop = k == I.maxIter;
-      if (I.useResidual && k >= 1) {
+      bool stop = k == maxIter;
+      if (useRes && k >= 1) {
         used = k;
         if (threadIdx.x == 0) {  // the only thread that reports them
           lastRes = gate;
-          if (I.resTrace && rank == 0) I.resTrace[(size_t)step * I.maxIter + k - 1] = gate;
+          if (resTraceP && rank == 0) resTraceP[(size_t)step * maxIter + k - 1] = gate;
         }
         conv = gateHit != 0;
         stop = stop || conv;
@@ -380,16 +418,21 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         break;
       }
 
-      // this CTA's rows of Ã⁻¹·r: groups of kGroupRows rows × column segments over the warps
-      for (int task = warp; task < groups * segs; task += kWarps) {
-        const int li = kGroupRows * (task / segs), sg = task - (task / segs) * segs;
-        const int jb = q4 * sg / segs, je = q4 * (sg + 1) / segs;
-        const int nr = min(kGroupRows, m - li);
-        float* out = dl + sg * 3 * chunk;
-        if (li < resRows) {  // resRows is a multiple of 4 unless it covers every row
-          rowGroup<kGroupRows, true>(As + static_cast<size_t>(li) * ld, nr, Rs, ld, li, jb, je, out);
-        } else {
-          rowGroup<kGroupRows, false>(I.Ainv + static_cast<size_t>(rb + li) * ld, nr, Rs, ld, li, jb, je, out);
+      // this CTA's rows of Ã⁻¹·r: blocks of up to kRowBlock rows, each applied by kDeltaProductWarps
+      // warps over interleaved columns (resident rows from shared memory, the rest through L2)
+      if (warp < kDeltaProductWarps) {
+        for (int li = 0; li < m;) {
+          const bool resident = li < resRows;
+          const int nr = min(kRowBlock, (resident ? resRows : m) - li);
+          float* out = dl + warp * 3 * chunk + 3 * li;
+          const float* A0 = resident ? As + static_cast<size_t>(li) * ld : I.Ainv + static_cast<size_t>(rb + li) * ld;
+          if (resident && nr == kRowBlock)
+            rowBlock<true, true>(A0, nr, Rs, ld, warp, kDeltaProductWarps, out);
+          else if (resident)
+            rowBlock<true, false>(A0, nr, Rs, ld, warp, kDeltaProductWarps, out);
+          else
+            rowBlock<false, false>(A0, nr, Rs, ld, warp, kDeltaProductWarps, out);
+          li += nr;
         }
       }
       __syncthreads();
@@ -401,7 +444,6 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         const int li = t / 3, c = t - 3 * li, v = rb + li;
         float hi = xf[8 * v + c], lo = xf[8 * v + 4 + c];
         if (sV[li].z != 0.f) {
-          const float* qf = reinterpret_cast<const float*>(I.qhl);
           const float qh = __ldg(qf + 8 * v + c), ql = __ldg(qf + 8 * v + 4 + c);
           const float d = (qh - hi) + (ql - lo);
           dmax = fmaxf(dmax, fabsf(om * d));
@@ -410,18 +452,19 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
           if (blend && !split) addHL(hi, lo, (om - 1.f) * d);
         } else {
           float d = dl[t];
-          for (int sgi = 1; sgi < segs; ++sgi) d += dl[sgi * 3 * chunk + t];
+#pragma unroll
+          for (int w = 1; w < kDeltaProductWarps; ++w) d += dl[w * 3 * chunk + t];
           dmax = fmaxf(dmax, fabsf(om * d));
           addHL(hi, lo, (blend && !split) ? om * d : d);
         }
-        storeRelaxed(I.xtag + 6 * v + c, tagged(tagB, hi));
-        storeRelaxed(I.xtag + 6 * v + 3 + c, tagged(tagB, lo));
+        storeRelaxed(xtag + 6 * v + c, tagged(tagB, hi));
+        storeRelaxed(xtag + 6 * v + 3 + c, tagged(tagB, lo));
       }
       // exchange B: the positions this CTA reads; with the displacement gate also the maximum of
       // the displacements (warp 0), which makes it a full barrier — with the residual gate a CTA
       // waits only for the CTAs owning its window
       __syncthreads();  // own positions are read back by other threads below
-      if (!I.useResidual) {
+      if (!useRes) {
         dmax = warpMaxF(dmax);
         if (lane == 0) red[warp] = dmax;
         __syncthreads();
@@ -433,19 +476,16 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
           }
           __syncwarp();
           ok = pollPartials(ptagB, team, tagB, &gate);
-          if (lane == 0) {  // the displacement gate's decision, once
-            const double diff = gate;
-            const double rel = (scale > 0.0) ? diff / scale : diff;
-            gateHit = ((I.absTol > 0.0) && (diff <= I.absTol)) || ((I.relTol > 0.0) && (rel <= I.relTol)) ? 1 : 0;
-          }
+          if (lane == 0)  // the displacement gate's decision, once, on thresholds taken at k = 0
+            gateHit = (gate <= dispAbsF) || (gate <= dispRelF) ? 1 : 0;
         } else {
-          ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
+          ok = pollWords<4>(xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x - 32, blockDim.x - 32, [&](int j, float val) {
             const int v = j / 6, c = j - 6 * v;  // c < 3: hi, else lo
             xf[8 * v + (c < 3 ? c : c + 1)] = val;
           });
         }
       } else {
-        ok = pollWords<4>(I.xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x, blockDim.x, [&](int j, float val) {
+        ok = pollWords<4>(xtag, 6 * wlo, 6 * whi, tagB, threadIdx.x, blockDim.x, [&](int j, float val) {
           const int v = j / 6, c = j - 6 * v;
           xf[8 * v + (c < 3 ? c : c + 1)] = val;
         });
@@ -486,7 +526,7 @@ __global__ void __launch_bounds__(kDeltaThreads, 1) substepDeltaKernel(const Ins
         }
         __syncthreads();
       }
-      if (!I.useResidual) {
+      if (!useRes) {
         used = k + 1;
         conv = gateHit != 0;
         if (conv) break;

@@ -23,9 +23,10 @@
 // neighbours and bend partners). An exchange word carries the epoch it was written in and its data,
 // written and polled with relaxed gpu-scope accesses: a position or a partial maximum travels as two
 // words (epoch << 32 | low or high 32 bits of the FP64), an r value as one packed word (packR). r and
-// the A partials alternate between two buffers.
-// Every poll gives up after a bounded number of rounds, sets the instance's error flag and ends the
-// CTA. Chebyshev-weighted iterates are not taken here (the planner keeps the supernodal kernel then).
+// the A partials alternate between two buffers. Polls do not sleep between rounds (a store is
+// visible to another SM ~250 ns later on the same die, ~370 ns on the other; each round waits for its
+// own loads). Every poll gives up after a bounded number of rounds, sets the instance's error flag and
+// ends the CTA. Chebyshev-weighted iterates are not taken here (the planner keeps the supernodal kernel then).
 // The same kernel serves PD_PRECISION_FP32_PROJECTION on small cloths: the projection d_e in FP32,
 // the correction, the solve and the residual as above.
 #include <cstdint>
@@ -76,7 +77,6 @@ __device__ __forceinline__ bool pollValues(const unsigned long long* src, int b,
 #pragma unroll
     for (int u = 0; u < B; ++u) lo[u] = hi[u] = 0u;
     long long spins = 0;
-    unsigned nap = 32;  // back off while words are stale, so waiting CTAs do not flood L2
     while (pending) {
       unsigned long long w[2 * B];
 #pragma unroll
@@ -92,11 +92,7 @@ __device__ __forceinline__ bool pollValues(const unsigned long long* src, int b,
           pending &= ~(1u << u);
         }
       }
-      if (pending) {
-        if (++spins > kSpinLimit) return false;
-        __nanosleep(nap);
-        nap = min(2 * nap, 256u);
-      }
+      if (pending && ++spins > kSpinLimit) return false;
     }
 #pragma unroll
     for (int u = 0; u < B; ++u)
@@ -131,7 +127,6 @@ __device__ __forceinline__ bool pollPacked(const unsigned long long* src, int b,
     for (int u = 0; u < B; ++u)
       if (j0 + u * nth < e) pending |= 1u << u;
     long long spins = 0;
-    unsigned nap = 32;
     while (pending) {
       unsigned long long w[B];
 #pragma unroll
@@ -144,11 +139,7 @@ __device__ __forceinline__ bool pollPacked(const unsigned long long* src, int b,
           pending &= ~(1u << u);
         }
       }
-      if (pending) {
-        if (++spins > kSpinLimit) return false;
-        __nanosleep(nap);
-        nap = min(2 * nap, 256u);
-      }
+      if (pending && ++spins > kSpinLimit) return false;
     }
   }
   return true;
@@ -179,7 +170,6 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
 #pragma unroll
   for (int i = 0; i < kMaxTeam / 32; ++i) lo[i] = hi[i] = 0u;
   long long spins = 0;
-  unsigned nap = 32;
   bool good = true;
   while (true) {
     unsigned long long w[2 * (kMaxTeam / 32)];
@@ -199,8 +189,6 @@ __device__ __forceinline__ bool pollPartials(const unsigned long long* ptag, int
       good = false;
       break;
     }
-    __nanosleep(nap);
-    nap = min(2 * nap, 256u);
   }
   long long mx = 0;
 #pragma unroll
