@@ -23,9 +23,17 @@
 namespace pdg {
 namespace {
 
-constexpr int kLanesPerVertex = 8;  // lanes sharing one vertex's incidences
+// Lanes sharing one vertex's incidences in the correction pass. The pass is bound by the latency of
+// its dependent loads (incidence records, then the neighbours' positions) once per round of vertices,
+// so fewer lanes a vertex — more vertices a round, fewer rounds — is faster where the team is small:
+// measured on the 512-cloth batch (one CTA or a 4-CTA cluster per cloth) 28.8 / 26.8 / 26.4 / 25.6 ms a
+// substep with 8 / 4 / 2 / 1 lanes, and on one 256×256 cloth over a 456-CTA grid 10.33 / 10.23 / 10.09 ms
+// with 8 / 4 / 2 (one lane costs the grid kernel registers and with them a third of its CTAs).
+constexpr int kLanesOneCta = 1;
+constexpr int kLanesCluster = 1;
+constexpr int kLanesGrid = 2;
 
-template <bool CLUSTER, bool TIMED = false>
+template <int LANES, bool CLUSTER, bool TIMED = false>
 __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, int substeps, float* Y, float* T,
                                 double* red, double* slots) {
   int parity = 0;
@@ -47,7 +55,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
   }
   tm.sync();
 
-  const int gl = TID & (kLanesPerVertex - 1), group = TID / kLanesPerVertex, ngroups = NT / kLanesPerVertex;
+  const int gl = TID & (LANES - 1), group = TID / LANES, ngroups = NT / LANES;
   const StageClock<TIMED> clk(I, TID == 0);
   for (int step = 0; step < substeps; ++step) {
     // predict (Integrator.cpp:447-472): x_n in FP64, x̂ as a pair
@@ -70,7 +78,7 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
     bool conv = false;
     double lastRes = I.useResidual ? 0.0 : -1.0;
     // correction b − Ã·x (elimination order, into Y when wanted) and the largest residual of the
-    // current positions, 8 lanes per vertex
+    // current positions, LANES lanes per vertex
     auto correctionPass = [&](bool wantY) {
       float res = 0.f;
       for (int base = 0; base < n; base += ngroups) {
@@ -81,10 +89,10 @@ __device__ void runSubstepsCorr(const InstanceDev& I, const Team<CLUSTER>& tm, i
         if (vc.z == 0.f) {
           const float4 vh = tm.ld(X + 2 * v), vl = tm.ld(X + 2 * v + 1);
           cs.accumulate<CLUSTER>(I, I.tEdge, I.rstart[v], I.rstart[v + 1], I.tBend, I.bstart[v], I.bstart[v + 1], X,
-                                 vh, vl, gl, kLanesPerVertex);
+                                 vh, vl, gl, LANES);
           if (gl == 0) cs.addMass(vh, vl, tm.ld(Xh + 2 * v), tm.ld(Xh + 2 * v + 1), vc.x);
         }
-        cs.reduce<kLanesPerVertex>();
+        cs.reduce<LANES>();
         if (active && gl == 0) {
           float3 r = make_float3(0.f, 0.f, 0.f);
           if (vc.z == 0.f) {
@@ -220,7 +228,7 @@ __global__ void __launch_bounds__(kBlockThreads, 4) substepCorrKernel(const Inst
   float* Y = inSmem ? sm : I.y32;
   float* T = inSmem ? sm + 3 * I.n : I.t32;
   const Team<false> tm{0, 1};
-  runSubstepsCorr<false, TIMED>(I, tm, substeps, Y, T, red, slots);
+  runSubstepsCorr<kLanesOneCta, false, TIMED>(I, tm, substeps, Y, T, red, slots);
 }
 
 template <bool TIMED>
@@ -232,7 +240,7 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrClusterKernel(const 
   const int cs = static_cast<int>(cl.num_blocks());
   const InstanceDev& I = insts[blockIdx.x / cs];
   const Team<true> tm{static_cast<int>(cl.block_rank()), cs};
-  runSubstepsCorr<true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
+  runSubstepsCorr<kLanesCluster, true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
 // A batch as a work table: resident CTAs of WT threads each take the next cloth from an integer
@@ -260,7 +268,7 @@ __global__ void __launch_bounds__(WT, 1024 / WT) substepCorrWorkKernel(const Ins
     float* Y = inSmem ? sm : I.y32;
     float* T = inSmem ? sm + 3 * I.n : I.t32;
     const Team<false> tm{0, 1};
-    runSubstepsCorr<false, TIMED>(I, tm, substeps, Y, T, red, slots);
+    runSubstepsCorr<kLanesOneCta, false, TIMED>(I, tm, substeps, Y, T, red, slots);
     __syncthreads();
   }
 }
@@ -276,7 +284,7 @@ __global__ void __launch_bounds__(kBlockThreads) substepCorrGridKernel(const Ins
   const InstanceDev& I = insts[0];
   Team<true> tm{static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x)};
   tm.gslots = I.w;
-  runSubstepsCorr<true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
+  runSubstepsCorr<kLanesGrid, true, TIMED>(I, tm, substeps, I.y32, I.t32, red, slots);
 }
 
 cudaLaunchConfig_t corrClusterConfig(int blocks, int cs, void* stream, cudaLaunchAttribute* attr) {
