@@ -826,6 +826,10 @@ struct pd_sim {
     const int want = wantCtas();
     int team = want > 0 ? want : sms / count;
     team = std::min({team, sms / count, minN, 256});  // 256: partials one polling warp covers
+    if (want <= 0 && count == 1) {  // the fewest CTAs with the same rows each: none is left without rows
+      const int chunk = (maxN + team - 1) / team;
+      team = (maxN + chunk - 1) / chunk;
+    }
     if (team < 2) return false;
     int smem = 0, rows = 0;
     for (const auto& I : inst) smem = std::max(smem, deltaSmem(I, team, &rows));
@@ -856,6 +860,10 @@ struct pd_sim {
     const int count = static_cast<int>(inst.size());
     int team = want > 0 ? want : sms / count;
     team = std::min({team, sms / count, minN, 256});  // 256: partials one polling warp covers
+    if (want <= 0 && count == 1) {  // the fewest CTAs with the same rows each: none is left without rows
+      const int chunk = (maxN + team - 1) / team;
+      team = (maxN + chunk - 1) / chunk;
+    }
     if (team < 2) return false;
     int smem = 0, rows = 0;
     for (const auto& I : inst) smem = std::max(smem, delta64Smem(I, team, &rows));
