@@ -316,7 +316,9 @@ int pd_sim_spectrum(pd_sim* s, int32_t instance, int32_t power_iterations, pd_sp
  * autotuner"; no counterpart in the reference, whose solve runs on host threads) ----
  * A plan overrides the planner's built-in choices; 0 keeps the built-in choice of a field. */
 typedef struct pd_plan {
-  int32_t team_ctas;         /* CTAs per cloth: the MIXED team kernel's team, or the thread-block
+  int32_t team_ctas;         /* CTAs per cloth: the team kernels' team (built-in: the SMs shared
+                                out over the cloths; one cloth's team trimmed to the CTAs that own
+                                rows, 146 for a 40×40 cloth on 152 SMs), or the thread-block
                                 cluster of the supernodal kernels (takes precedence over
                                 pd_scene_config.cluster_ctas) */
   int32_t big_min_vertices;  /* MIXED batches above the explicit-inverse limit: cloths of at least
