@@ -28,9 +28,11 @@ namespace {
 // so fewer lanes a vertex — more vertices a round, fewer rounds — is faster where the team is small:
 // measured on the 512-cloth batch (one CTA or a 4-CTA cluster per cloth) 28.8 / 26.8 / 26.4 / 25.6 ms a
 // substep with 8 / 4 / 2 / 1 lanes, and on one 256×256 cloth over a 456-CTA grid 10.33 / 10.23 / 10.09 ms
-// with 8 / 4 / 2 (one lane costs the grid kernel registers and with them a third of its CTAs).
+// with 8 / 4 / 2 (one lane costs the grid kernel registers and with them a third of its CTAs). The
+// cluster kernel takes two: with one it needs 128 registers a thread and fits two CTAs an SM; the
+// autotuned batch (8-CTA clusters for the large cloths) 23.4 ms a substep with one lane, 20.8 with two.
 constexpr int kLanesOneCta = 1;
-constexpr int kLanesCluster = 1;
+constexpr int kLanesCluster = 2;
 constexpr int kLanesGrid = 2;
 
 template <int LANES, bool CLUSTER, bool TIMED = false>
